@@ -1,0 +1,262 @@
+/*
+ * plsqr_gpu.h — C ABI of the GB300 PLSQR3 operator and LSQR driver.
+ *
+ * The library replaces, on one GPU, the hot path of PLSQR3:
+ *   - the operator  aprod(version, procRank, numProc, mode, m, n, x, y,
+ *     UsrWrk, isFinalIteration, iteration)             source/aprod.h:10-13
+ *     (mode 1: y <- y + A x, mode 2: x <- x + A^T y, A = [K; D]),
+ *   - the driver    lsqr(..., aprod, damp, UsrWrk, u, v, w, x, se, atol,
+ *     btol, conlim, itnlim, nout, outputs..., lsqr_iteration) source/lsqr.h:32-62,
+ *   - the loaders of the kernel and damping binary/info files and the result
+ *     writer (source/plsqr3.c:1008-1626, 1986-2013), single partition.
+ *
+ * Conventions: every function returns 0 (PLSQR_OK) or a negative PLSQR_ERR_*
+ * code and never exits the process (the reference calls exit(-1) / MPI_Abort
+ * on the same conditions).  Matrices and vectors are FP64 (the reference with
+ * SDVERSION=2) and indices are 0-based int32 with int32 or int64 pointer
+ * arrays.  A context owns all of its device memory and one CUDA stream; it is
+ * not reentrant (like the reference's function-static scratch), so use one
+ * context per host thread.  No type in these signatures depends on CUDA.
+ */
+#ifndef PLSQR_GPU_H
+#define PLSQR_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLSQR_GPU_ABI_VERSION 1
+
+/* ---- error codes ------------------------------------------------------- */
+#define PLSQR_OK 0
+#define PLSQR_ERR_ARG (-1)      /* invalid argument or size                    */
+#define PLSQR_ERR_IO (-2)       /* file cannot be opened, read or written      */
+#define PLSQR_ERR_FORMAT (-3)   /* file or matrix content is inconsistent      */
+#define PLSQR_ERR_NOMEM (-4)    /* host allocation failed                      */
+#define PLSQR_ERR_CUDA (-5)     /* CUDA runtime error (device memory, launch)  */
+#define PLSQR_ERR_NODEV (-6)    /* no usable CUDA device                       */
+#define PLSQR_ERR_STATE (-7)    /* call out of sequence                        */
+#define PLSQR_ERR_TIMEOUT (-8)  /* a bounded device wait gave up               */
+#define PLSQR_ERR_INTERNAL (-9) /* internal consistency check failed           */
+#define PLSQR_ERR_NUMERIC (-10) /* NaN or Inf in an input vector               */
+
+/* source/main.h:26-36 precision switch, as a run-time choice */
+#define PLSQR_PREC_FP64 0  /* FP64 values, vectors, reductions              */
+#define PLSQR_PREC_MIXED 1 /* FP32 inner sweeps on the value split, FP64 outer */
+
+/* Compressed sparse matrix, by column (ptr over columns, idx = row) or by
+ * row (ptr over rows, idx = column); SpMatCSC / SpMatCSR of
+ * source/main.h:123-130, 158-165.  Exactly one of ptr32 / ptr64 is set, so
+ * the reference's own int* col_ptr can be passed without a copy. */
+typedef struct {
+  int32_t num_row;
+  int32_t num_col;
+  int64_t nnz;
+  const int32_t *ptr32;
+  const int64_t *ptr64;
+  const int32_t *idx;
+  const double *val;
+} plsqr_sparse;
+
+/* The reference command line (source/plsqr3.c:105-186): file names are
+ * relative to dir; -row_ptn / -col_ptn have no meaning on one partition. */
+typedef struct {
+  const char *dir;
+  const char *ker_f;        /* -ker_f  kernel records, sorted by column     */
+  const char *ker_i;        /* -ker_i  ASCII "col nnz start", 1-based       */
+  const char *damp_f;       /* -damp_f damping records, sorted by row       */
+  const char *damp_i;       /* -damp_i int32 nnz per damping row            */
+  const char *damp_f_bycol; /* -damp_f_bycol damping records, by column     */
+  const char *damp_i_bycol; /* -damp_i_bycol int32 nnz per column           */
+  const char *b_k;          /* -b_k    ASCII measurement vector             */
+  int32_t row_k, row_d, col;
+} plsqr_files;
+
+typedef struct {
+  int32_t device;    /* CUDA device ordinal (default 0)                       */
+  int32_t precision; /* PLSQR_PREC_*                                          */
+  int32_t use_graph; /* capture each LSQR iteration as a CUDA graph (def. 1)  */
+  int32_t verbose;   /* print the per-iteration alpha/beta lines like lsqr.c  */
+} plsqr_opts;
+
+typedef struct {
+  int32_t m_k, m_d, n;
+  int64_t nnz_k, nnz_d;
+  int64_t device_bytes;       /* device memory held by the context        */
+  int32_t sm_count;
+  double hbm_bytes_aprod1;    /* algorithmic bytes of one mode-1 aprod    */
+  double hbm_bytes_aprod2;    /* algorithmic bytes of one mode-2 aprod    */
+  double hbm_bytes_iteration; /* algorithmic bytes of one LSQR iteration  */
+} plsqr_info;
+
+/* Arguments of lsqr() (source/lsqr.h:32-62); call_lsqr uses damp = 0,
+ * atol = btol = 1e-10, conlim = 100, itnlim = 1000 (source/lsqr.c:47-51). */
+typedef struct {
+  double damp, atol, btol, conlim;
+  int32_t itnlim;
+  int32_t lsqr_iteration; /* iterations run; istop does not stop the loop,
+                             as in source/lsqr.c:829-834                      */
+  int32_t want_se;        /* compute the standard-error estimate se[]        */
+  int32_t stop_on_istop;  /* 0 = reference behaviour                         */
+  const char *result_txt; /* NULL, or path of the Paige-Saunders log written
+                             like result.txt (source/lsqr.c:246-268, 780-905) */
+  /* PLSQR_PREC_MIXED contexts only: `sweeps` outer refinement steps, each
+   * an FP32 LSQR of `inner` iterations on r = b - A x (FP64); the history
+   * then holds sweeps * inner + 1 records and lsqr_iteration is unused.     */
+  int32_t sweeps, inner;
+} plsqr_lsqr_args;
+
+/* Scalars of one iteration (index 0 = start-up, source/lsqr.c:343-445). */
+typedef struct {
+  double alpha, beta, rnorm, arnorm, test1, test2, anorm, acond, xnorm, x0;
+  double err; /* ||x - x_ref|| / ||x_ref|| when a reference x is set, else -1 */
+  int32_t istop, pad;
+} plsqr_iter;
+
+/* Outputs of lsqr() (source/lsqr.c:908-914; arnorm_out is test2 there). */
+typedef struct {
+  int32_t istop, itn;
+  double anorm, acond, rnorm, arnorm_out, xnorm;
+  double arnorm, bnorm, dxmax;
+  int32_t maxdx, pad;
+  double seconds; /* device time of the iteration loop (CUDA events) */
+} plsqr_result;
+
+typedef struct plsqr_ctx plsqr_ctx;
+
+/* ---- library ----------------------------------------------------------- */
+const char *plsqr_strerror(int code);
+int plsqr_abi_version(void);
+void plsqr_default_opts(plsqr_opts *opts);
+void plsqr_default_lsqr_args(plsqr_lsqr_args *args);
+/* Number of CUDA devices; 0 and PLSQR_OK when the driver has none. */
+int plsqr_device_count(int32_t *count);
+
+/* ---- context: replaces PLSQR3_main's loading + initPPDataV3_TRI +
+ *      InitPPDataV3_TRI_GPU (source/plsqr3.c:218-575, tridiagonal.c:13-95,
+ *      lsqr.c:455) ------------------------------------------------------- */
+/* From the matrices in the reference's in-memory layout: K by column
+ * (matCSC_k), D by row (matCSR_d) and D by column (matCSC_d_bycol).  The
+ * kernel matrix is also transposed to rows on the device. */
+int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
+                     const plsqr_sparse *d_csc, const plsqr_opts *opts,
+                     plsqr_ctx **out);
+/* From the reference's files; b_k is loaded too (plsqr3.c:580-589). */
+int plsqr_ctx_create_files(const plsqr_files *files, const plsqr_opts *opts,
+                           plsqr_ctx **out);
+/* FinalPPDataV3_TRI_GPU (source/lsqr.c:873). NULL is accepted. */
+void plsqr_ctx_destroy(plsqr_ctx *ctx);
+int plsqr_ctx_info(const plsqr_ctx *ctx, plsqr_info *info);
+/* Last CUDA error text seen by the context (empty if none). */
+const char *plsqr_ctx_last_error(const plsqr_ctx *ctx);
+
+/* ---- vectors of PPDataV3_TRI: u = [vec_y_k; vec_y_d], v = vec_x -------- */
+int plsqr_set_u(plsqr_ctx *ctx, const double *y_k, const double *y_d);
+int plsqr_get_u(plsqr_ctx *ctx, double *y_k, double *y_d);
+int plsqr_set_v(plsqr_ctx *ctx, const double *v);
+int plsqr_get_v(plsqr_ctx *ctx, double *v);
+/* b_k loaded by plsqr_ctx_create_files (or NULL-safe copy out). */
+int plsqr_get_b(plsqr_ctx *ctx, double *b_k);
+
+/* ---- operator ---------------------------------------------------------- */
+/* aprod on the device-resident vectors: mode 1 y += A x, mode 2 x += A^T y
+ * (source/aprod.c:24-84, aprod_impl.c:22-524).  iteration and is_final have
+ * the reference's meaning and do not change the result. */
+int plsqr_aprod(plsqr_ctx *ctx, int mode, int iteration, int is_final);
+/* The same with host vectors, the drop-in for the reference call: the input
+ * vectors are copied to the device, the updated one is copied back
+ * (mode 1 reads x, updates y_k/y_d; mode 2 reads y_k/y_d, updates x). */
+int plsqr_aprod_host(plsqr_ctx *ctx, int mode, double *y_k, double *y_d,
+                     double *x, int iteration, int is_final);
+
+/* ---- driver ------------------------------------------------------------ */
+/* lsqr() on the device (source/lsqr.c:195-917).  b_k (host, m_k values; NULL
+ * = the b_k the context loaded) is the right-hand side, the damping part of
+ * b is zero.  x, w, se (host, n values each) may be NULL; hist may be NULL or
+ * hold lsqr_iteration + 1 records. */
+int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k,
+               double *x, double *w, double *se, plsqr_iter *hist,
+               plsqr_result *res);
+/* A reference solution (host, n values) against which every iteration
+ * records ||x - x_ref|| / ||x_ref|| in plsqr_iter.err; NULL clears it. */
+int plsqr_set_reference_x(plsqr_ctx *ctx, const double *x_ref);
+/* The last solution x (host, n values). */
+int plsqr_get_x(plsqr_ctx *ctx, double *x);
+/* mpiio_write_result (source/plsqr3.c:1986-2013): raw FP64 x[n]. */
+int plsqr_write_result(plsqr_ctx *ctx, const char *path);
+
+/* ---- files, host side (no GPU needed) ----------------------------------- */
+/* read_kernel_col_info (plsqr3.c:1379-1409): nnz[n], start[n] (0-based,
+ * -1 where the file has 0) and the total. */
+int plsqr_io_read_kernel_info(const char *path, int32_t n, int32_t *nnz,
+                              int64_t *start, int64_t *total);
+/* mpiio_load_kernelColBin2CSC_once (plsqr3.c:1515-1626): K by column. */
+int plsqr_io_read_kernel(const char *bin_path, const char *info_path,
+                         int32_t m_k, int32_t n, int64_t *col_ptr,
+                         int32_t *row_idx, double *val);
+/* mpiio_load_damp_info (plsqr3.c:1008-1025) and the column info read at
+ * plsqr3.c:503-508: int32 counts, returns their sum in *total. */
+int plsqr_io_read_int32_counts(const char *path, int64_t count, int32_t *out,
+                               int64_t *total);
+/* mpiio_load_damp_once (plsqr3.c:1027-1194), CSR (by_col = 0) or CSC. */
+int plsqr_io_read_damping(const char *bin_path, int by_col, int32_t m_d,
+                          int32_t n, int64_t nnz, int64_t *ptr, int32_t *idx,
+                          double *val);
+/* b_k, ASCII %le one per line (plsqr3.c:580-589). */
+int plsqr_io_read_rhs(const char *path, int32_t m_k, double *b_k);
+/* Writers of the same formats (the PLSQR3_tools outputs:
+ * Ker2PLSQR3.c:499-608, damping_binary.py:75-616). */
+int plsqr_io_write_kernel(const char *bin_path, const char *info_path,
+                          int32_t m_k, int32_t n, const int64_t *col_ptr,
+                          const int32_t *row_idx, const double *val);
+int plsqr_io_write_damping(const char *row_bin, const char *row_info,
+                           const char *col_bin, const char *col_info,
+                           int32_t m_d, int32_t n, const int64_t *row_ptr,
+                           const int32_t *col_idx, const double *val,
+                           const int64_t *col_ptr, const int32_t *row_idx,
+                           const double *cval);
+int plsqr_io_write_rhs(const char *path, int32_t m_k, const double *b_k);
+int plsqr_io_write_x(const char *path, int32_t n, const double *x);
+
+/* ---- synthetic problems and helpers, host side ------------------------- */
+typedef struct {
+  int32_t nx, ny, nz;       /* grid; column = iz*ny*nx + iy*nx + ix          */
+  int32_t n_rays;           /* kernel rows                                   */
+  double tube_radius;       /* cells within this distance of the ray         */
+  int32_t face_axis;        /* rays join the two faces normal to this axis;
+                               -1 = a random axis per ray                    */
+  int32_t n_blobs;          /* Gaussian blobs in x_true                      */
+  double value_scale;       /* kernel value = |N(0,1)| * value_scale         */
+  double blob_sigma;        /* blob width in cells                           */
+  double checker_amp;       /* checkerboard amplitude (0 = none)             */
+  int32_t checker_period;   /* checkerboard period in cells                  */
+  int32_t pad;
+  double noise_frac;        /* noise sigma / rms(K x_true)                   */
+  double damp_identity;     /* identity damping weight                       */
+  double damp_lap;          /* second-difference damping weight              */
+  uint64_t seed;
+} plsqr_synth_params;
+
+void plsqr_synth_default_params(plsqr_synth_params *p);
+int plsqr_synth_kernel_counts(const plsqr_synth_params *p, int64_t *row_ptr);
+int plsqr_synth_kernel_fill(const plsqr_synth_params *p, const int64_t *row_ptr,
+                            int32_t *col_idx, double *val);
+int plsqr_synth_damping_size(const plsqr_synth_params *p, int64_t *m_d,
+                             int64_t *nnz_d);
+int plsqr_synth_damping_fill(const plsqr_synth_params *p, int64_t *row_ptr,
+                             int32_t *col_idx, double *val);
+int plsqr_synth_xtrue(const plsqr_synth_params *p, double *x);
+int plsqr_synth_rhs(const plsqr_synth_params *p, const int64_t *row_ptr,
+                    const int32_t *col_idx, const double *val,
+                    const double *xtrue, double *b);
+/* CSR <-> CSC transpose; output lines keep ascending input-line order. */
+int plsqr_transpose(int64_t n_lines, int64_t n_out, const int64_t *ptr,
+                    const int32_t *idx, const double *val, int64_t *tptr,
+                    int32_t *tidx, double *tval);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PLSQR_GPU_H */

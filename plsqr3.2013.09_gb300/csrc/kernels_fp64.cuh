@@ -1,0 +1,383 @@
+// FP64 kernels of one LSQR iteration on the GB300 (sm_103a).
+//
+// The operator A = [K; D] is held four ways so that both products are
+// gathers (no atomics, deterministic):
+//   K by row    (k_rp, k_ci, k_v)   A x, kernel part   (transposed on device)
+//   D by row    (d_rp, d_ci, d_v)   A x, damping part
+//   K by column (kc_p, kc_ri, kc_v) A^T y, kernel part
+//   D by column (dc_p, dc_ri, dc_v) A^T y, damping part
+// u = [y_k; y_d] is one array of m = m_k + m_d values.
+//
+// Kernel rows and columns hold thousands of nonzeros: one warp streams a
+// row with 16-byte loads (4 indices, 2x2 values per lane and step) and
+// reduces with shuffles.  Damping rows hold at most 3 nonzeros and damping
+// columns at most 10: one thread sums them sequentially in stored order, as
+// the reference does (CPUSpMV.c:63-72, 267-277).
+//
+// Reductions (norms, dknorm, error) write one partial per block; the next
+// kernel sums the partials in a fixed order, so results do not depend on
+// scheduling, and no kernel waits on another block.
+#pragma once
+
+#include "lsqr_state.cuh"
+
+namespace plsqr {
+
+// Sum of val[e] * x[idx[e]] over [beg, end) by one warp; the result is valid
+// in every lane.
+__device__ __forceinline__ double warp_dot_f64(const int32_t *__restrict__ idx,
+                                               const double *__restrict__ val,
+                                               const double *__restrict__ x, int64_t beg,
+                                               int64_t end, int lane) {
+  double acc0 = 0.0, acc1 = 0.0;
+  // head: up to 3 elements until beg is a multiple of 4
+  int64_t a4 = (beg + 3) & ~int64_t(3);
+  if (a4 > end) a4 = end;
+  if (beg + lane < a4) acc0 = val[beg + lane] * x[idx[beg + lane]];
+  const int64_t e4 = a4 + ((end - a4) & ~int64_t(3));
+  // body: groups of 4 aligned elements, lane-strided; two groups in flight
+  const int4 *__restrict__ idx4 = reinterpret_cast<const int4 *>(idx);
+  const double2 *__restrict__ val2 = reinterpret_cast<const double2 *>(val);
+  int64_t g = (a4 >> 2) + lane;
+  const int64_t gend = e4 >> 2;
+  for (; g + 32 < gend; g += 64) {
+    const int4 c0 = __ldg(idx4 + g), c1 = __ldg(idx4 + g + 32);
+    const double2 v0 = __ldg(val2 + 2 * g), v1 = __ldg(val2 + 2 * g + 1);
+    const double2 w0 = __ldg(val2 + 2 * (g + 32)), w1 = __ldg(val2 + 2 * (g + 32) + 1);
+    acc0 = fma(v0.x, __ldg(x + c0.x), acc0);
+    acc1 = fma(v0.y, __ldg(x + c0.y), acc1);
+    acc0 = fma(v1.x, __ldg(x + c0.z), acc0);
+    acc1 = fma(v1.y, __ldg(x + c0.w), acc1);
+    acc0 = fma(w0.x, __ldg(x + c1.x), acc0);
+    acc1 = fma(w0.y, __ldg(x + c1.y), acc1);
+    acc0 = fma(w1.x, __ldg(x + c1.z), acc0);
+    acc1 = fma(w1.y, __ldg(x + c1.w), acc1);
+  }
+  if (g < gend) {
+    const int4 c0 = __ldg(idx4 + g);
+    const double2 v0 = __ldg(val2 + 2 * g), v1 = __ldg(val2 + 2 * g + 1);
+    acc0 = fma(v0.x, __ldg(x + c0.x), acc0);
+    acc1 = fma(v0.y, __ldg(x + c0.y), acc1);
+    acc0 = fma(v1.x, __ldg(x + c0.z), acc0);
+    acc1 = fma(v1.y, __ldg(x + c0.w), acc1);
+  }
+  // tail: up to 3 elements
+  if (e4 + lane < end) acc1 = fma(val[e4 + lane], x[idx[e4 + lane]], acc1);
+  double s = acc0 + acc1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+// Sequential sum in stored order, mul and add rounded separately.
+__device__ __forceinline__ double seq_dot_f64(const int32_t *__restrict__ idx,
+                                              const double *__restrict__ val,
+                                              const double *__restrict__ x, int64_t beg,
+                                              int64_t end) {
+  double t = 0.0;
+  for (int64_t e = beg; e < end; ++e) t = dadd(t, dmul(val[e], x[idx[e]]));
+  return t;
+}
+
+template <int kThreads>
+__device__ __forceinline__ double block_sum(double v, double *smem) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) smem[warp] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < kThreads / 32 ? smem[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  }
+  return s;  // valid in thread 0
+}
+
+// Sum of parts[0..n) in a fixed order; valid in thread 0.  Every block that
+// calls it on the same data gets the same bits.
+template <int kThreads>
+__device__ __forceinline__ double sum_parts(const double *parts, int n, double *smem) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += kThreads) v += parts[i];
+  return block_sum<kThreads>(v, smem);
+}
+
+// Scale applied to the old vector in the fused products:
+enum ScaleMode : int {
+  kScaleOne = 0,       // plain aprod: y += A x
+  kScaleNegAlpha = 1,  // LSQR mode 1: u = -alpha u + A v
+  kScaleNegBeta = 2,   // LSQR mode 2: v = -beta v + A^T u (skipped if beta == 0)
+  kScaleZero = 3,      // LSQR start-up: v = 0 + A^T u
+};
+
+// ---------------------------------------------------------------------------
+// M1: u_k[r] = s*u_k[r] + (K v)[r], u_d[r] = s*u_d[r] + (D v)[r]; per-block
+// partial sums of squares of the new u: parts[0..gk) kernel rows,
+// parts[gk..gk+gd) damping rows.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_aprod1(Csr K, Csr D, const double *__restrict__ v, double *__restrict__ u, int gk,
+             int mode, const DevState *__restrict__ st, double *__restrict__ parts) {
+  __shared__ double smem[kThreads / 32];
+  double s = 1.0;
+  if (mode == kScaleNegAlpha) s = -st->alpha;
+  double sq = 0.0;
+  if ((int)blockIdx.x < gk) {
+    const int lane = threadIdx.x & 31;
+    const int warps_total = gk * (kThreads / 32);
+    for (int r = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); r < K.n_lines;
+         r += warps_total) {
+      const double t = warp_dot_f64(K.idx, K.val, v, K.ptr[r], K.ptr[r + 1], lane);
+      if (lane == 0) {
+        const double y = dadd(dmul(s, u[r]), t);  // dscal, then y_k += t_k
+        u[r] = y;
+        sq = fma(y, y, sq);
+      }
+    }
+  } else {
+    const int gd = gridDim.x - gk;
+    double *ud = u + K.n_lines;
+    for (int r = (blockIdx.x - gk) * kThreads + threadIdx.x; r < D.n_lines;
+         r += gd * kThreads) {
+      const double t = seq_dot_f64(D.idx, D.val, v, D.ptr[r], D.ptr[r + 1]);
+      const double y = dadd(dmul(s, ud[r]), t);
+      ud[r] = y;
+      sq = fma(y, y, sq);
+    }
+  }
+  const double b = block_sum<kThreads>(sq, smem);
+  if (threadIdx.x == 0 && parts) parts[blockIdx.x] = b;
+}
+
+// ---------------------------------------------------------------------------
+// N1: beta = sqrt(sum_k + sum_d); u *= 1/beta.  LSQR start-up (start = 1)
+// also takes this path with beta = ||b||.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_norm_u(double *__restrict__ u, int64_t m, const double *__restrict__ parts, int gk,
+             int gd, DevState *__restrict__ st, int start) {
+  __shared__ double smem[kThreads / 32];
+  __shared__ double s_rb;
+  const double sk = sum_parts<kThreads>(parts, gk, smem);
+  const double sd = sum_parts<kThreads>(parts + gk, gd, smem);
+  if (threadIdx.x == 0) {
+    const double beta = __dsqrt_rn(dadd(sk, sd));
+    s_rb = beta > 0.0 ? ddiv(1.0, beta) : 0.0;
+    if (blockIdx.x == 0) {
+      st->beta = beta;
+      st->s_beta_pos = beta > 0.0;
+      if (!start) {  // source/lsqr.c:526-528
+        double temp = d2norm(st->alpha, beta);
+        temp = d2norm(temp, st->damp);
+        st->anorm = d2norm(st->anorm, temp);
+      }
+    }
+  }
+  __syncthreads();
+  const double rb = s_rb;
+  if (rb == 0.0) return;  // beta == 0: u is left as is
+  for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * kThreads)
+    u[i] = dmul(u[i], rb);
+}
+
+// ---------------------------------------------------------------------------
+// M2: v[c] = s*v[c] + ((K^T u_k)[c] + (D^T u_d)[c]); per-block partial sum of
+// squares of the new v.  In LSQR mode the whole kernel is skipped when
+// beta == 0 (source/lsqr.c:530).
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_aprod2(Csr KC, Csr DC, const double *__restrict__ u, int m_k, double *__restrict__ v,
+             int mode, const DevState *__restrict__ st, double *__restrict__ parts) {
+  __shared__ double smem[kThreads / 32];
+  double s = 1.0;
+  if (mode == kScaleNegBeta) {
+    if (!st->s_beta_pos) return;
+    s = -st->beta;
+  } else if (mode == kScaleZero) {
+    if (!st->s_beta_pos) return;
+    s = 0.0;
+  }
+  const double *ud = u + m_k;
+  const int lane = threadIdx.x & 31;
+  const int warps_total = gridDim.x * (kThreads / 32);
+  double sq = 0.0;
+  for (int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); c < KC.n_lines;
+       c += warps_total) {
+    const double sk = warp_dot_f64(KC.idx, KC.val, u, KC.ptr[c], KC.ptr[c + 1], lane);
+    if (lane == 0) {
+      const double sd = seq_dot_f64(DC.idx, DC.val, ud, DC.ptr[c], DC.ptr[c + 1]);
+      const double y = dadd(dmul(s, v[c]), dadd(sk, sd));  // x += (s_k + s_d)
+      v[c] = y;
+      sq = fma(y, y, sq);
+    }
+  }
+  const double b = block_sum<kThreads>(sq, smem);
+  if (threadIdx.x == 0 && parts) parts[blockIdx.x] = b;
+}
+
+// ---------------------------------------------------------------------------
+// N2: alpha = ||v||, v *= 1/alpha, then the rotation and the x/w update
+// (source/lsqr.c:577-692).  Writes per-block partials of dknorm^2 to
+// parts_dk and of ||x - x_ref||^2 to parts_err.  start = 1: the LSQR start-up
+// (source/lsqr.c:375-445): w = v, x = 0, no rotation.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_update_x(double *__restrict__ v, double *__restrict__ w, double *__restrict__ x,
+               double *__restrict__ se, const double *__restrict__ xref, int n,
+               const double *__restrict__ parts, int gp, DevState *__restrict__ st,
+               double *__restrict__ parts_dk, double *__restrict__ parts_err,
+               plsqr_iter *__restrict__ hist, int start) {
+  __shared__ double smem[kThreads / 32];
+  __shared__ double s_alpha, s_ra;
+  __shared__ Step s_step;
+  const int beta_pos = st->s_beta_pos;
+  const double vv = beta_pos ? sum_parts<kThreads>(parts, gp, smem) : 0.0;
+  if (threadIdx.x == 0) {
+    double alpha = st->alpha;  // unchanged when beta == 0
+    if (beta_pos) alpha = __dsqrt_rn(vv);
+    if (start && !beta_pos) alpha = 0.0;
+    s_alpha = alpha;
+    s_ra = (beta_pos && alpha > 0.0) ? ddiv(1.0, alpha) : 0.0;
+    if (!start) s_step = lsqr_step(*st, alpha, st->beta);
+  }
+  __syncthreads();
+  const double ra = s_ra;
+  if (start) {
+    for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+      double vi = v[i];
+      if (ra != 0.0) vi = dmul(vi, ra);
+      v[i] = vi;
+      w[i] = ra != 0.0 ? vi : 0.0;  // w = v only when alpha > 0 (lsqr.c:392-395)
+      x[i] = 0.0;
+      if (se) se[i] = 0.0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      const double alpha = s_alpha, beta = st->beta;
+      st->alpha = alpha;
+      st->arnorm = dmul(alpha, beta);
+      st->rhobar = alpha;
+      st->phibar = beta;
+      st->bnorm = beta;
+      st->rnorm = beta;
+      st->done = st->arnorm == 0.0;
+      if (hist) {
+        plsqr_iter &h = hist[0];
+        h.alpha = alpha;
+        h.beta = beta;
+        h.rnorm = beta;
+        h.arnorm = st->arnorm;
+        h.test1 = 1.0;
+        h.test2 = beta > 0.0 ? ddiv(alpha, beta) : 0.0;
+        h.anorm = 0.0;
+        h.acond = 0.0;
+        h.xnorm = 0.0;
+        h.x0 = 0.0;
+        h.err = st->has_ref ? 1.0 : -1.0;
+        h.istop = 0;
+        h.pad = 0;
+      }
+    }
+    return;
+  }
+  const Step sp = s_step;
+  double dk = 0.0, e2 = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double vi = v[i];
+    if (ra != 0.0) {
+      vi = dmul(vi, ra);
+      v[i] = vi;
+    }
+    const double t = w[i];
+    const double xi = dadd(dmul(sp.t1, t), x[i]);
+    x[i] = xi;
+    w[i] = dadd(dmul(sp.t2, t), vi);
+    const double tt = dmul(dmul(sp.t3, t), dmul(sp.t3, t));
+    if (se) se[i] = dadd(tt, se[i]);
+    dk += tt;
+    if (xref) {
+      const double d = xi - xref[i];
+      e2 = fma(d, d, e2);
+    }
+  }
+  const double bdk = block_sum<kThreads>(dk, smem);
+  const double be2 = xref ? block_sum<kThreads>(e2, smem) : 0.0;
+  if (threadIdx.x == 0) {
+    parts_dk[blockIdx.x] = bdk;
+    if (parts_err) parts_err[blockIdx.x] = be2;
+    if (blockIdx.x == 0) {
+      st->s_alpha = s_alpha;
+      st->s_rhobar = sp.rhobar;
+      st->s_phibar = sp.phibar;
+      st->s_psi = sp.psi;
+      st->s_phi = sp.phi;
+      st->s_rho = sp.rho;
+      st->s_theta = sp.theta;
+      st->s_tau = sp.tau;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// T: the rest of the iteration's scalars and the history record (one block).
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_tail(DevState *__restrict__ st, const double *__restrict__ parts_dk,
+           const double *__restrict__ parts_err, int gp, const double *__restrict__ x,
+           plsqr_iter *__restrict__ hist) {
+  __shared__ double smem[kThreads / 32];
+  const double dk = sum_parts<kThreads>(parts_dk, gp, smem);
+  const double e2 = parts_err ? sum_parts<kThreads>(parts_err, gp, smem) : 0.0;
+  if (threadIdx.x == 0) lsqr_tail(*st, dk, e2, x[0], hist);
+}
+
+// ---------------------------------------------------------------------------
+// Sum of squares of u = [y_k; y_d] (kernel part in blocks [0, gk), damping
+// part in [gk, grid)), for the start-up beta = ||b||.
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_sumsq_u(const double *__restrict__ u, int m_k, int64_t m_d, int gk,
+              double *__restrict__ parts) {
+  __shared__ double smem[kThreads / 32];
+  double sq = 0.0;
+  if ((int)blockIdx.x < gk) {
+    for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < m_k;
+         i += (int64_t)gk * kThreads)
+      sq = fma(u[i], u[i], sq);
+  } else {
+    const int gd = gridDim.x - gk;
+    for (int64_t i = (blockIdx.x - gk) * (int64_t)kThreads + threadIdx.x; i < m_d;
+         i += (int64_t)gd * kThreads)
+      sq = fma(u[m_k + i], u[m_k + i], sq);
+  }
+  const double b = block_sum<kThreads>(sq, smem);
+  if (threadIdx.x == 0) parts[blockIdx.x] = b;
+}
+
+// ||x_ref||^2 into st->ref_norm2 (one block).
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_ref_norm(const double *__restrict__ xref, int n, DevState *__restrict__ st) {
+  __shared__ double smem[kThreads / 32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += kThreads) s = fma(xref[i], xref[i], s);
+  const double b = block_sum<kThreads>(s, smem);
+  if (threadIdx.x == 0) st->ref_norm2 = b;
+}
+
+// se[i] = t * sqrt(se[i]) (source/lsqr.c:878-891)
+static __global__ void k_finish_se(double *__restrict__ se, int n, const DevState *__restrict__ st,
+                            int num_row) {
+  const double rnorm = st->rnorm;
+  double t = 1.0;
+  if (num_row > n) t = (double)(num_row - n);
+  if (st->damp > 0.0) t = (double)num_row;
+  t = ddiv(rnorm, __dsqrt_rn(t));
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    se[i] = dmul(t, __dsqrt_rn(se[i]));
+}
+
+}  // namespace plsqr

@@ -1,0 +1,231 @@
+// Mixed-precision LSQR: iterative refinement with FP32 inner sweeps.
+//
+//   x = 0
+//   repeat `sweeps` times:
+//     r  = [b_k; 0] - A x                   FP64, kernel values hi + lo
+//     dx = LSQR(A_hi, r), `inner` iterations FP32 vectors, FP64 scalars/norms
+//     x += dx                               FP64
+//
+// The least-squares correction problem min ||A dx - r|| has the solution
+// x* - x, so every sweep contracts the error by the factor the inner sweep
+// reaches.  The inner iteration is the five-kernel iteration of the FP64
+// solver with FP32 vectors and 8-byte kernel nonzeros (kernels_f32.cuh),
+// captured once as a CUDA graph.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "kernels_f32.cuh"
+#include "plsqr_internal.h"
+
+using namespace plsqr;
+
+namespace {
+constexpr int kThreads = 256;
+}
+
+struct MixedState {
+  float *k_hi = nullptr, *k_lo = nullptr, *kc_hi = nullptr;
+  float *uf = nullptr, *vf = nullptr, *wf = nullptr, *dxf = nullptr;
+  double *b = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_key = -1;
+  plsqr_iter *graph_hist = nullptr;
+};
+
+#define CK(call)                                                                 \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess) {                                                     \
+      ctx_set_error(ctx, "%s:%d %s: %s", __FILE__, __LINE__, #call,              \
+                    cudaGetErrorString(e_));                                     \
+      return PLSQR_ERR_CUDA;                                                     \
+    }                                                                            \
+  } while (0)
+
+void mixed_free(plsqr_ctx *ctx) {
+  if (!ctx || !ctx->mixed) return;
+  if (ctx->mixed->graph) cudaGraphExecDestroy(ctx->mixed->graph);
+  delete ctx->mixed;  // device buffers are in ctx->allocs
+  ctx->mixed = nullptr;
+}
+
+int mixed_prepare(plsqr_ctx *ctx) {
+  if (ctx->mixed) return PLSQR_OK;
+  ctx->mixed = new MixedState();
+  MixedState *M = ctx->mixed;
+  int rc;
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  if ((rc = dev_alloc(ctx, &M->k_hi, (size_t)ctx->nnz_k)) ||
+      (rc = dev_alloc(ctx, &M->k_lo, (size_t)ctx->nnz_k)) ||
+      (rc = dev_alloc(ctx, &M->kc_hi, (size_t)ctx->nnz_k)) ||
+      (rc = dev_alloc(ctx, &M->uf, (size_t)m)) || (rc = dev_alloc(ctx, &M->vf, (size_t)ctx->n)) ||
+      (rc = dev_alloc(ctx, &M->wf, (size_t)ctx->n)) ||
+      (rc = dev_alloc(ctx, &M->dxf, (size_t)ctx->n)) ||
+      (rc = dev_alloc(ctx, &M->b, (size_t)std::max(ctx->m_k, 1))))
+    return rc;
+  const int g = ctx->sm_count * 8;
+  k_split_hilo<<<g, 256, 0, ctx->stream>>>(ctx->K.val, ctx->nnz_k, M->k_hi, M->k_lo);
+  k_split_hilo<<<g, 256, 0, ctx->stream>>>(ctx->KC.val, ctx->nnz_k, M->kc_hi, nullptr);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PLSQR_OK;
+}
+
+static CsrF rows_f(const plsqr_ctx *ctx) {
+  return CsrF{ctx->K.ptr, ctx->K.idx, ctx->mixed->k_hi, ctx->mixed->k_lo, ctx->K.n_lines};
+}
+static CsrF cols_f(const plsqr_ctx *ctx) {
+  return CsrF{ctx->KC.ptr, ctx->KC.idx, ctx->mixed->kc_hi, nullptr, ctx->KC.n_lines};
+}
+
+static int enqueue_inner(plsqr_ctx *ctx, cudaStream_t s) {
+  MixedState *M = ctx->mixed;
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  const double *xref = ctx->has_ref ? ctx->xref : nullptr;
+  k_aprod1_f32<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
+      rows_f(ctx), ctx->D.csr(), M->vf, M->uf, ctx->g1k, ctx->st, ctx->parts_u);
+  k_norm_u_f32<kThreads><<<ctx->gvu, kThreads, 0, s>>>(M->uf, m, ctx->parts_u, ctx->g1k, ctx->g1d,
+                                                       ctx->st);
+  k_aprod2_f32<kThreads><<<ctx->g2, kThreads, 0, s>>>(cols_f(ctx), ctx->DC.csr(), M->uf, ctx->m_k,
+                                                       M->vf, 0, ctx->st, ctx->parts_v);
+  k_update_dx_f32<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
+      M->vf, M->wf, M->dxf, ctx->x, xref, ctx->n, ctx->parts_v, ctx->g2, ctx->st, ctx->parts_dk,
+      xref ? ctx->parts_err : nullptr, 0);
+  k_tail<kThreads><<<1, kThreads, 0, s>>>(ctx->st, ctx->parts_dk, xref ? ctx->parts_err : nullptr,
+                                           ctx->gvx, ctx->x, ctx->hist);
+  CK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
+static int ensure_inner_graph(plsqr_ctx *ctx) {
+  MixedState *M = ctx->mixed;
+  const int key = ctx->has_ref ? 1 : 0;
+  if (M->graph && M->graph_key == key && M->graph_hist == ctx->hist) return PLSQR_OK;
+  if (M->graph) cudaGraphExecDestroy(M->graph);
+  M->graph = nullptr;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_inner(ctx, ctx->stream);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  CK(e);
+  e = cudaGraphInstantiate(&M->graph, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  M->graph_key = key;
+  M->graph_hist = ctx->hist;
+  return PLSQR_OK;
+}
+
+int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, double *x,
+               double *w, double *se, plsqr_iter *hist, plsqr_result *res) {
+  (void)w;
+  (void)se;
+  if (args->sweeps < 1 || args->inner < 1 || args->want_se) return PLSQR_ERR_ARG;
+  int rc;
+  if ((rc = mixed_prepare(ctx))) return rc;
+  MixedState *M = ctx->mixed;
+  const double *b = b_k;
+  if (!b) {
+    if ((int32_t)ctx->b_k.size() != ctx->m_k) return PLSQR_ERR_STATE;
+    b = ctx->b_k.data();
+  }
+  CK(cudaSetDevice(ctx->opts.device));
+  const int S = args->sweeps, I = args->inner;
+  const int total = S * I;
+  if (ctx->hist_cap < total + 1) {
+    if (ctx->hist) dev_free(ctx, ctx->hist);
+    ctx->hist = nullptr;
+    if ((rc = dev_alloc(ctx, &ctx->hist, (size_t)total + 1))) return rc;
+    ctx->hist_cap = total + 1;
+  }
+  if (ctx->m_k > 0)
+    CK(cudaMemcpyAsync(M->b, b, sizeof(double) * ctx->m_k, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->n, ctx->stream));
+  CK(cudaMemsetAsync(ctx->hist, 0, sizeof(plsqr_iter) * (total + 1), ctx->stream));
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  std::vector<plsqr_iter> hh((size_t)total + 1);
+  DevState cur;
+  memset(&cur, 0, sizeof(cur));
+  int done_sweeps = 0, last_itn = 0;
+  if ((rc = ensure_inner_graph(ctx))) return rc;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int s = 0; s < S; ++s) {
+    DevState h;
+    memset(&h, 0, sizeof(h));
+    h.damp = args->damp;
+    h.atol = args->atol;
+    h.btol = args->btol;
+    h.ctol = args->conlim > 0.0 ? 1.0 / args->conlim : 0.0;
+    h.itnlim = args->itnlim;
+    h.has_ref = ctx->has_ref;
+    h.cs2 = -1.0;
+    h.hist_base = s * I;
+    CK(cudaMemcpyAsync(ctx->st, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+    if (ctx->has_ref) k_ref_norm<kThreads><<<1, kThreads, 0, ctx->stream>>>(ctx->xref, ctx->n, ctx->st);
+    // outer residual and the start-up of the inner solve
+    k_residual<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, ctx->stream>>>(
+        rows_f(ctx), ctx->D.csr(), ctx->x, M->b, ctx->u, ctx->g1k, ctx->parts_u);
+    k_norm_u<kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, ctx->parts_u, ctx->g1k,
+                                                                ctx->g1d, ctx->st, 1);
+    k_to_f32<<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, M->uf);
+    k_aprod2_f32<kThreads><<<ctx->g2, kThreads, 0, ctx->stream>>>(
+        cols_f(ctx), ctx->DC.csr(), M->uf, ctx->m_k, M->vf, 1, ctx->st, ctx->parts_v);
+    k_update_dx_f32<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
+        M->vf, M->wf, M->dxf, ctx->x, nullptr, ctx->n, ctx->parts_v, ctx->g2, ctx->st,
+        ctx->parts_dk, nullptr, 1);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (s == 0) {
+      plsqr_iter &h0 = hh[0];
+      h0.alpha = cur.alpha;
+      h0.beta = cur.beta;
+      h0.rnorm = cur.beta;
+      h0.arnorm = cur.arnorm;
+      h0.test1 = 1.0;
+      h0.test2 = cur.beta > 0.0 ? cur.alpha / cur.beta : 0.0;
+      h0.err = ctx->has_ref ? 1.0 : -1.0;
+    }
+    if (cur.done) break;  // A^T r = 0: x is a least-squares solution
+    for (int i = 0; i < I; ++i) CK(cudaGraphLaunch(M->graph, ctx->stream));
+    k_add_dx<<<ctx->gvx, kThreads, 0, ctx->stream>>>(ctx->x, M->dxf, ctx->n);
+    CK(cudaGetLastError());
+    done_sweeps = s + 1;
+    last_itn = (s + 1) * I;
+  }
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(hh.data() + 1, ctx->hist + 1, sizeof(plsqr_iter) * total,
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  if (x) CK(cudaMemcpyAsync(x, ctx->x, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->solved = true;
+  (void)done_sweeps;
+  plsqr_result r;
+  memset(&r, 0, sizeof(r));
+  r.istop = cur.istop;
+  r.itn = last_itn;
+  r.anorm = cur.anorm;
+  r.acond = cur.acond;
+  r.rnorm = cur.rnorm;
+  r.arnorm_out = cur.test2;
+  r.xnorm = cur.xnorm;
+  r.arnorm = cur.arnorm;
+  r.bnorm = cur.bnorm;
+  r.dxmax = cur.dxmax;
+  r.maxdx = cur.maxdx;
+  r.seconds = ms * 1e-3;
+  if (res) *res = r;
+  if (hist) memcpy(hist, hh.data(), sizeof(plsqr_iter) * (total + 1));
+  return PLSQR_OK;
+}

@@ -1,0 +1,640 @@
+// GB300 PLSQR3: device context, the aprod operator and the LSQR driver
+// behind the C ABI of include/plsqr_gpu.h.
+//
+// One context holds the operator in four layouts (kernel and damping matrix,
+// by row and by column; the kernel rows are built on the device from the
+// by-column input), the LSQR vectors u = [y_k; y_d], v, w, x (and se), the
+// scalar state and the per-iteration history, all in device memory.  One LSQR
+// iteration is five kernels (kernels_fp64.cuh) captured once as a CUDA graph
+// and replayed; the host only enqueues graph launches and reads results back
+// at the end.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "kernels_fp64.cuh"
+#include "plsqr_internal.h"
+#include "transpose.cuh"
+
+using namespace plsqr;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+const char *const kErrText[] = {
+    "success",
+    "invalid argument or size",
+    "file cannot be opened, read or written",
+    "file or matrix content is inconsistent",
+    "host allocation failed",
+    "CUDA runtime error",
+    "no usable CUDA device",
+    "call out of sequence",
+    "a bounded device wait gave up",
+    "internal consistency check failed",
+    "NaN or Inf in an input vector",
+};
+
+}  // namespace
+
+#define CK(call)                                                               \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ctx_set_error(ctx, "%s:%d %s: %s", __FILE__, __LINE__, #call,            \
+                    cudaGetErrorString(e_));                                   \
+      return PLSQR_ERR_CUDA;                                                   \
+    }                                                                          \
+  } while (0)
+
+void ctx_set_error(plsqr_ctx *ctx, const char *fmt, ...) {
+  if (!ctx) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(ctx->last_error, sizeof(ctx->last_error), fmt, ap);
+  va_end(ap);
+}
+
+int ctx_dev_alloc_bytes(plsqr_ctx *ctx, void **p, size_t bytes) {
+  *p = nullptr;
+  CK(cudaMalloc(p, bytes));
+  ctx->allocs.emplace_back(*p, bytes);
+  ctx->device_bytes += (int64_t)bytes;
+  return PLSQR_OK;
+}
+
+void ctx_dev_free(plsqr_ctx *ctx, void *p) {
+  if (!p) return;
+  for (size_t i = 0; i < ctx->allocs.size(); ++i)
+    if (ctx->allocs[i].first == p) {
+      ctx->device_bytes -= (int64_t)ctx->allocs[i].second;
+      ctx->allocs.erase(ctx->allocs.begin() + (long)i);
+      break;
+    }
+  cudaFree(p);
+}
+
+// ---------------------------------------------------------------------------
+// host-side validation of a compressed sparse matrix (no device fault can
+// come from a bad index: every index is checked before upload)
+static int validate_sparse(const plsqr_sparse *a, int32_t rows, int32_t cols, int by_col,
+                           std::vector<int64_t> &ptr64) {
+  if (!a || (!a->ptr32 && !a->ptr64) || (a->ptr32 && a->ptr64)) return PLSQR_ERR_ARG;
+  if (a->num_row != rows || a->num_col != cols || a->nnz < 0) return PLSQR_ERR_ARG;
+  const int32_t n_lines = by_col ? cols : rows, n_idx = by_col ? rows : cols;
+  ptr64.resize((size_t)n_lines + 1);
+  for (int32_t i = 0; i <= n_lines; ++i) ptr64[i] = a->ptr32 ? (int64_t)a->ptr32[i] : a->ptr64[i];
+  if (ptr64[0] != 0 || ptr64[n_lines] != a->nnz) return PLSQR_ERR_FORMAT;
+  for (int32_t i = 0; i < n_lines; ++i)
+    if (ptr64[i + 1] < ptr64[i]) return PLSQR_ERR_FORMAT;
+  if (a->nnz > 0 && (!a->idx || !a->val)) return PLSQR_ERR_ARG;
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t e = 0; e < a->nnz; ++e)
+    if (a->idx[e] < 0 || a->idx[e] >= n_idx) bad = 1;
+  return bad ? PLSQR_ERR_FORMAT : PLSQR_OK;
+}
+
+static int upload_lines(plsqr_ctx *ctx, const plsqr_sparse *a, const std::vector<int64_t> &ptr,
+                        DevLines *out, int32_t n_lines) {
+  int rc;
+  if ((rc = dev_alloc(ctx, &out->ptr, (size_t)n_lines + 1))) return rc;
+  if ((rc = dev_alloc(ctx, &out->idx, (size_t)a->nnz))) return rc;
+  if ((rc = dev_alloc(ctx, &out->val, (size_t)a->nnz))) return rc;
+  CK(cudaMemcpy(out->ptr, ptr.data(), ((size_t)n_lines + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+  if (a->nnz > 0) {
+    CK(cudaMemcpy(out->idx, a->idx, (size_t)a->nnz * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(out->val, a->val, (size_t)a->nnz * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  out->n_lines = n_lines;
+  out->nnz = a->nnz;
+  return PLSQR_OK;
+}
+
+// K by row from K by column, on the device (transpose.cuh)
+static int build_kernel_rows(plsqr_ctx *ctx) {
+  const int m = ctx->m_k, n = ctx->n;
+  int rc;
+  if ((rc = dev_alloc(ctx, &ctx->K.ptr, (size_t)m + 1))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->K.idx, (size_t)ctx->nnz_k))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->K.val, (size_t)ctx->nnz_k))) return rc;
+  ctx->K.n_lines = m;
+  ctx->K.nnz = ctx->nnz_k;
+  if (m == 0) {
+    CK(cudaMemset(ctx->K.ptr, 0, sizeof(int64_t)));
+    return PLSQR_OK;
+  }
+  // chunk count: enough blocks to fill the GPU, bounded by 2 GiB of cursors
+  int64_t nb = std::min<int64_t>((int64_t)ctx->sm_count * 4, std::max(n, 1));
+  nb = std::min<int64_t>(nb, std::max<int64_t>(1, (int64_t)(2LL << 30) / (12LL * m)));
+  int32_t *cnt = nullptr;
+  int64_t *cur = nullptr, *rowcnt = nullptr;
+  if ((rc = dev_alloc(ctx, &cnt, (size_t)(nb * m)))) return rc;
+  if ((rc = dev_alloc(ctx, &cur, (size_t)(nb * m)))) return rc;
+  if ((rc = dev_alloc(ctx, &rowcnt, (size_t)m))) return rc;
+  CK(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * nb * m, ctx->stream));
+  k_tr_count<<<(int)nb, 256, 0, ctx->stream>>>(ctx->KC.ptr, ctx->KC.idx, n, (int)nb, m, cnt);
+  k_tr_rowtot<<<std::max(1, std::min(4096, (m + 255) / 256)), 256, 0, ctx->stream>>>(cnt, (int)nb, m, rowcnt);
+  k_scan_one_block<<<1, 1024, 0, ctx->stream>>>(rowcnt, m, ctx->K.ptr);
+  k_tr_cursor<<<std::max(1, std::min(4096, (m + 255) / 256)), 256, 0, ctx->stream>>>(cnt, (int)nb, m, ctx->K.ptr, cur);
+  k_tr_scatter<<<(int)nb, 256, 0, ctx->stream>>>(ctx->KC.ptr, ctx->KC.idx, ctx->KC.val, n, (int)nb, m,
+                                                (unsigned long long *)cur, ctx->K.idx, ctx->K.val);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  int64_t total = -1;
+  CK(cudaMemcpy(&total, ctx->K.ptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost));
+  dev_free(ctx, cnt);
+  dev_free(ctx, cur);
+  dev_free(ctx, rowcnt);
+  return total == ctx->nnz_k ? PLSQR_OK : PLSQR_ERR_INTERNAL;
+}
+
+static void plan_launch(plsqr_ctx *ctx) {
+  const int sm = ctx->sm_count;
+  const int wpb = kThreads / 32;
+  // mode 1: warps over kernel rows, threads over damping rows
+  ctx->g1k = std::max(1, std::min(sm * ctx->blocks_per_sm, (ctx->m_k + wpb - 1) / wpb));
+  ctx->g1d = std::max(1, std::min(sm * 2, (ctx->m_d + kThreads - 1) / kThreads));
+  // mode 2: warps over columns
+  ctx->g2 = std::max(1, std::min(sm * ctx->blocks_per_sm, (ctx->n + wpb - 1) / wpb));
+  // vector kernels
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  ctx->gvu = (int)std::max<int64_t>(1, std::min<int64_t>(sm * 4, (m + kThreads - 1) / kThreads));
+  ctx->gvx = std::max(1, std::min(sm * 4, (ctx->n + kThreads - 1) / kThreads));
+  ctx->gsk = std::max(1, std::min(sm, (ctx->m_k + kThreads - 1) / kThreads));
+  ctx->gsd = std::max(1, std::min(sm, (ctx->m_d + kThreads - 1) / kThreads));
+}
+
+static void free_graph(plsqr_ctx *ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  ctx->graph_exec = nullptr;
+}
+
+static int ctx_init_common(plsqr_ctx *ctx) {
+  CK(cudaSetDevice(ctx->opts.device));
+  CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&ctx->ev0));
+  CK(cudaEventCreate(&ctx->ev1));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, ctx->opts.device));
+  ctx->sm_count = prop.multiProcessorCount;
+  if (ctx->blocks_per_sm <= 0) ctx->blocks_per_sm = 8;
+  const char *env = getenv("PLSQR_BLOCKS_PER_SM");
+  if (env && atoi(env) > 0) ctx->blocks_per_sm = atoi(env);
+  return PLSQR_OK;
+}
+
+static int ctx_alloc_vectors(plsqr_ctx *ctx) {
+  int rc;
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  if ((rc = dev_alloc(ctx, &ctx->u, (size_t)m))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->v, (size_t)ctx->n))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->w, (size_t)ctx->n))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->x, (size_t)ctx->n))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->parts_u, kMaxParts))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->parts_v, kMaxParts))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->parts_dk, kMaxParts))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->parts_err, kMaxParts))) return rc;
+  if ((rc = dev_alloc(ctx, &ctx->st, 1))) return rc;
+  CK(cudaMemset(ctx->u, 0, sizeof(double) * std::max<int64_t>(m, 1)));
+  CK(cudaMemset(ctx->v, 0, sizeof(double) * std::max(ctx->n, 1)));
+  CK(cudaMemset(ctx->w, 0, sizeof(double) * std::max(ctx->n, 1)));
+  CK(cudaMemset(ctx->x, 0, sizeof(double) * std::max(ctx->n, 1)));
+  CK(cudaMemset(ctx->st, 0, sizeof(DevState)));
+  return PLSQR_OK;
+}
+
+static double algorithmic_bytes(const plsqr_ctx *ctx, int mode) {
+  // bytes a perfect kernel moves: matrix entries (int32 index + FP64 value),
+  // pointer arrays, the vector it updates read and written once, the gathered
+  // vector read once (it stays in L2)
+  const double mk = ctx->m_k, md = ctx->m_d, n = ctx->n;
+  if (mode == 1)
+    return 12.0 * ((double)ctx->nnz_k + (double)ctx->nnz_d) + 8.0 * (mk + 1 + md + 1) +
+           16.0 * (mk + md) + 8.0 * n;
+  return 12.0 * ((double)ctx->nnz_k + (double)ctx->nnz_d) + 16.0 * (n + 1) + 16.0 * n +
+         8.0 * (mk + md);
+}
+
+extern "C" {
+
+const char *plsqr_strerror(int code) {
+  const int i = -code;
+  if (i < 0 || i >= (int)(sizeof(kErrText) / sizeof(kErrText[0]))) return "unknown error";
+  return kErrText[i];
+}
+
+int plsqr_abi_version(void) { return PLSQR_GPU_ABI_VERSION; }
+
+void plsqr_default_opts(plsqr_opts *o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->device = 0;
+  o->precision = PLSQR_PREC_FP64;
+  o->use_graph = 1;
+  o->verbose = 0;
+}
+
+void plsqr_default_lsqr_args(plsqr_lsqr_args *a) {
+  if (!a) return;
+  memset(a, 0, sizeof(*a));
+  a->damp = 0.0;  // source/lsqr.c:47-51
+  a->atol = 1e-10;
+  a->btol = 1e-10;
+  a->conlim = 100;
+  a->itnlim = 1000;
+  a->lsqr_iteration = 100;
+  a->sweeps = 4;
+  a->inner = 50;
+}
+
+int plsqr_device_count(int32_t *count) {
+  if (!count) return PLSQR_ERR_ARG;
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    c = 0;
+  }
+  *count = c;
+  return PLSQR_OK;
+}
+
+void plsqr_ctx_destroy(plsqr_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->opts.device);
+  free_graph(ctx);
+  mixed_free(ctx);
+  for (auto &a : ctx->allocs) cudaFree(a.first);
+  ctx->allocs.clear();
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
+                     const plsqr_sparse *d_csc, const plsqr_opts *opts, plsqr_ctx **out) {
+  if (!out || !k_csc || !d_csr || !d_csc) return PLSQR_ERR_ARG;
+  *out = nullptr;
+  const int32_t m_k = k_csc->num_row, n = k_csc->num_col, m_d = d_csr->num_row;
+  if (m_k < 0 || n < 1 || m_d < 0 || (int64_t)m_k + m_d < 1) return PLSQR_ERR_ARG;
+  std::vector<int64_t> kp, dp, dcp;
+  int rc;
+  if ((rc = validate_sparse(k_csc, m_k, n, 1, kp))) return rc;
+  if ((rc = validate_sparse(d_csr, m_d, n, 0, dp))) return rc;
+  if ((rc = validate_sparse(d_csc, m_d, n, 1, dcp))) return rc;
+  if (d_csc->nnz != d_csr->nnz) return PLSQR_ERR_FORMAT;
+  int32_t ndev = 0;
+  plsqr_device_count(&ndev);
+  plsqr_opts o;
+  plsqr_default_opts(&o);
+  if (opts) o = *opts;
+  if (ndev < 1 || o.device < 0 || o.device >= ndev) return PLSQR_ERR_NODEV;
+
+  plsqr_ctx *ctx = new plsqr_ctx();
+  ctx->opts = o;
+  ctx->m_k = m_k;
+  ctx->m_d = m_d;
+  ctx->n = n;
+  ctx->nnz_k = k_csc->nnz;
+  ctx->nnz_d = d_csr->nnz;
+  if ((rc = ctx_init_common(ctx)) || (rc = upload_lines(ctx, k_csc, kp, &ctx->KC, n)) ||
+      (rc = upload_lines(ctx, d_csr, dp, &ctx->D, m_d)) ||
+      (rc = upload_lines(ctx, d_csc, dcp, &ctx->DC, n)) || (rc = build_kernel_rows(ctx)) ||
+      (rc = ctx_alloc_vectors(ctx))) {
+    plsqr_ctx_destroy(ctx);
+    return rc;
+  }
+  plan_launch(ctx);
+  if (o.precision == PLSQR_PREC_MIXED && (rc = mixed_prepare(ctx))) {
+    plsqr_ctx_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return PLSQR_OK;
+}
+
+int plsqr_ctx_info(const plsqr_ctx *ctx, plsqr_info *info) {
+  if (!ctx || !info) return PLSQR_ERR_ARG;
+  memset(info, 0, sizeof(*info));
+  info->m_k = ctx->m_k;
+  info->m_d = ctx->m_d;
+  info->n = ctx->n;
+  info->nnz_k = ctx->nnz_k;
+  info->nnz_d = ctx->nnz_d;
+  info->device_bytes = ctx->device_bytes;
+  info->sm_count = ctx->sm_count;
+  info->hbm_bytes_aprod1 = algorithmic_bytes(ctx, 1);
+  info->hbm_bytes_aprod2 = algorithmic_bytes(ctx, 2);
+  // one iteration: both products plus the vector kernels (u scaled in place,
+  // v scaled and x, w updated: 8 bytes read + written per element)
+  const double m = (double)ctx->m_k + ctx->m_d, n = ctx->n;
+  info->hbm_bytes_iteration = info->hbm_bytes_aprod1 + info->hbm_bytes_aprod2 + 16.0 * m +
+                              8.0 * (2.0 * n + 4.0 * n);
+  return PLSQR_OK;
+}
+
+const char *plsqr_ctx_last_error(const plsqr_ctx *ctx) { return ctx ? ctx->last_error : ""; }
+
+static int check_finite(const double *p, int64_t n) {
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t i = 0; i < n; ++i)
+    if (!isfinite(p[i])) bad = 1;
+  return bad ? PLSQR_ERR_NUMERIC : PLSQR_OK;
+}
+
+int plsqr_set_u(plsqr_ctx *ctx, const double *y_k, const double *y_d) {
+  if (!ctx || (!y_k && ctx->m_k > 0)) return PLSQR_ERR_ARG;
+  int rc;
+  if ((rc = check_finite(y_k, ctx->m_k))) return rc;
+  if (y_d && (rc = check_finite(y_d, ctx->m_d))) return rc;
+  CK(cudaSetDevice(ctx->opts.device));
+  if (ctx->m_k > 0)
+    CK(cudaMemcpyAsync(ctx->u, y_k, sizeof(double) * ctx->m_k, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->m_d > 0) {
+    if (y_d)
+      CK(cudaMemcpyAsync(ctx->u + ctx->m_k, y_d, sizeof(double) * ctx->m_d, cudaMemcpyHostToDevice,
+                         ctx->stream));
+    else
+      CK(cudaMemsetAsync(ctx->u + ctx->m_k, 0, sizeof(double) * ctx->m_d, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PLSQR_OK;
+}
+
+int plsqr_get_u(plsqr_ctx *ctx, double *y_k, double *y_d) {
+  if (!ctx) return PLSQR_ERR_ARG;
+  CK(cudaSetDevice(ctx->opts.device));
+  if (y_k && ctx->m_k > 0)
+    CK(cudaMemcpyAsync(y_k, ctx->u, sizeof(double) * ctx->m_k, cudaMemcpyDeviceToHost, ctx->stream));
+  if (y_d && ctx->m_d > 0)
+    CK(cudaMemcpyAsync(y_d, ctx->u + ctx->m_k, sizeof(double) * ctx->m_d, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PLSQR_OK;
+}
+
+int plsqr_set_v(plsqr_ctx *ctx, const double *v) {
+  if (!ctx || !v) return PLSQR_ERR_ARG;
+  int rc;
+  if ((rc = check_finite(v, ctx->n))) return rc;
+  CK(cudaSetDevice(ctx->opts.device));
+  CK(cudaMemcpyAsync(ctx->v, v, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PLSQR_OK;
+}
+
+int plsqr_get_v(plsqr_ctx *ctx, double *v) {
+  if (!ctx || !v) return PLSQR_ERR_ARG;
+  CK(cudaSetDevice(ctx->opts.device));
+  CK(cudaMemcpyAsync(v, ctx->v, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PLSQR_OK;
+}
+
+int plsqr_get_b(plsqr_ctx *ctx, double *b_k) {
+  if (!ctx || !b_k) return PLSQR_ERR_ARG;
+  if ((int32_t)ctx->b_k.size() != ctx->m_k) return PLSQR_ERR_STATE;
+  memcpy(b_k, ctx->b_k.data(), sizeof(double) * ctx->m_k);
+  return PLSQR_OK;
+}
+
+// Enqueue one product on the context's stream.
+static int launch_aprod(plsqr_ctx *ctx, int mode, int scale_mode, bool with_parts) {
+  if (mode == 1) {
+    k_aprod1<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, ctx->stream>>>(
+        ctx->K.csr(), ctx->D.csr(), ctx->v, ctx->u, ctx->g1k, scale_mode, ctx->st,
+        with_parts ? ctx->parts_u : nullptr);
+  } else {
+    k_aprod2<kThreads><<<ctx->g2, kThreads, 0, ctx->stream>>>(
+        ctx->KC.csr(), ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, scale_mode, ctx->st,
+        with_parts ? ctx->parts_v : nullptr);
+  }
+  CK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
+int plsqr_aprod(plsqr_ctx *ctx, int mode, int iteration, int is_final) {
+  (void)iteration;
+  (void)is_final;
+  if (!ctx || (mode != 1 && mode != 2)) return PLSQR_ERR_ARG;
+  CK(cudaSetDevice(ctx->opts.device));
+  int rc = launch_aprod(ctx, mode, kScaleOne, false);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PLSQR_OK;
+}
+
+int plsqr_aprod_host(plsqr_ctx *ctx, int mode, double *y_k, double *y_d, double *x,
+                     int iteration, int is_final) {
+  if (!ctx || (mode != 1 && mode != 2) || !x || (!y_k && ctx->m_k > 0) ||
+      (!y_d && ctx->m_d > 0))
+    return PLSQR_ERR_ARG;
+  int rc;
+  if ((rc = plsqr_set_u(ctx, y_k, y_d)) || (rc = plsqr_set_v(ctx, x)) ||
+      (rc = plsqr_aprod(ctx, mode, iteration, is_final)))
+    return rc;
+  return mode == 1 ? plsqr_get_u(ctx, y_k, y_d) : plsqr_get_v(ctx, x);
+}
+
+int plsqr_set_reference_x(plsqr_ctx *ctx, const double *x_ref) {
+  if (!ctx) return PLSQR_ERR_ARG;
+  CK(cudaSetDevice(ctx->opts.device));
+  if (!x_ref) {
+    ctx->has_ref = false;
+    return PLSQR_OK;
+  }
+  int rc;
+  if ((rc = check_finite(x_ref, ctx->n))) return rc;
+  if (!ctx->xref && (rc = dev_alloc(ctx, &ctx->xref, (size_t)ctx->n))) return rc;
+  CK(cudaMemcpy(ctx->xref, x_ref, sizeof(double) * ctx->n, cudaMemcpyHostToDevice));
+  ctx->has_ref = true;
+  return PLSQR_OK;
+}
+
+// Enqueue one LSQR iteration (source/lsqr.c:487-775): five kernels.
+static int enqueue_iteration(plsqr_ctx *ctx, cudaStream_t s) {
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  double *se = ctx->want_se ? ctx->se : nullptr;
+  const double *xref = ctx->has_ref ? ctx->xref : nullptr;
+  k_aprod1<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
+      ctx->K.csr(), ctx->D.csr(), ctx->v, ctx->u, ctx->g1k, kScaleNegAlpha, ctx->st, ctx->parts_u);
+  k_norm_u<kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d,
+                                                     ctx->st, 0);
+  k_aprod2<kThreads><<<ctx->g2, kThreads, 0, s>>>(ctx->KC.csr(), ctx->DC.csr(), ctx->u, ctx->m_k,
+                                                   ctx->v, kScaleNegBeta, ctx->st, ctx->parts_v);
+  k_update_x<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
+      ctx->v, ctx->w, ctx->x, se, xref, ctx->n, ctx->parts_v, ctx->g2, ctx->st, ctx->parts_dk,
+      xref ? ctx->parts_err : nullptr, ctx->hist, 0);
+  k_tail<kThreads><<<1, kThreads, 0, s>>>(ctx->st, ctx->parts_dk, xref ? ctx->parts_err : nullptr,
+                                           ctx->gvx, ctx->x, ctx->hist);
+  CK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
+static int ensure_graph(plsqr_ctx *ctx) {
+  const int key = (ctx->want_se ? 1 : 0) | (ctx->has_ref ? 2 : 0);
+  if (ctx->graph_exec && ctx->graph_key == key && ctx->graph_hist == ctx->hist) return PLSQR_OK;
+  free_graph(ctx);
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_iteration(ctx, ctx->stream);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  CK(e);
+  e = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  ctx->graph_key = key;
+  ctx->graph_hist = ctx->hist;
+  return PLSQR_OK;
+}
+
+int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, double *x,
+               double *w, double *se, plsqr_iter *hist, plsqr_result *res) {
+  if (!ctx || !args || args->lsqr_iteration < 0) return PLSQR_ERR_ARG;
+  if (ctx->opts.precision == PLSQR_PREC_MIXED)
+    return mixed_lsqr(ctx, args, b_k, x, w, se, hist, res);
+  const double *b = b_k;
+  if (!b) {
+    if ((int32_t)ctx->b_k.size() != ctx->m_k) return PLSQR_ERR_STATE;
+    b = ctx->b_k.data();
+  }
+  int rc;
+  CK(cudaSetDevice(ctx->opts.device));
+  const int itn = args->lsqr_iteration;
+  if (ctx->hist_cap < itn + 1) {
+    if (ctx->hist) dev_free(ctx, ctx->hist);
+    ctx->hist = nullptr;
+    if ((rc = dev_alloc(ctx, &ctx->hist, (size_t)itn + 1))) return rc;
+    ctx->hist_cap = itn + 1;
+  }
+  ctx->want_se = args->want_se != 0;
+  if (ctx->want_se && !ctx->se && (rc = dev_alloc(ctx, &ctx->se, (size_t)ctx->n))) return rc;
+
+  // lsqr.c:278-295 and the u = b, v = 0 set-up (plsqr3.c:580-603, lsqr.c:311-312)
+  if ((rc = plsqr_set_u(ctx, b, nullptr))) return rc;
+  CK(cudaMemsetAsync(ctx->v, 0, sizeof(double) * ctx->n, ctx->stream));
+  CK(cudaMemsetAsync(ctx->hist, 0, sizeof(plsqr_iter) * (itn + 1), ctx->stream));
+  DevState h;
+  memset(&h, 0, sizeof(h));
+  h.damp = args->damp;
+  h.atol = args->atol;
+  h.btol = args->btol;
+  h.ctol = args->conlim > 0.0 ? 1.0 / args->conlim : 0.0;
+  h.itnlim = args->itnlim;
+  h.want_se = ctx->want_se;
+  h.has_ref = ctx->has_ref;
+  h.cs2 = -1.0;
+  CK(cudaMemcpyAsync(ctx->st, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->has_ref) k_ref_norm<kThreads><<<1, kThreads, 0, ctx->stream>>>(ctx->xref, ctx->n, ctx->st);
+
+  // start-up: beta u = b, alpha v = A^T u (lsqr.c:343-445)
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  k_sumsq_u<kThreads><<<ctx->gsk + ctx->gsd, kThreads, 0, ctx->stream>>>(ctx->u, ctx->m_k, ctx->m_d,
+                                                                          ctx->gsk, ctx->parts_u);
+  k_norm_u<kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, ctx->parts_u, ctx->gsk,
+                                                              ctx->gsd, ctx->st, 1);
+  if ((rc = launch_aprod(ctx, 2, kScaleZero, true))) return rc;
+  k_update_x<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
+      ctx->v, ctx->w, ctx->x, ctx->want_se ? ctx->se : nullptr, nullptr, ctx->n, ctx->parts_v,
+      ctx->g2, ctx->st, ctx->parts_dk, nullptr, ctx->hist, 1);
+  CK(cudaGetLastError());
+  DevState cur;
+  CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+
+  int done_itn = 0;
+  float ms = 0.f;
+  if (!cur.done && itn > 0) {
+    const bool graph = ctx->opts.use_graph != 0;
+    if (graph && (rc = ensure_graph(ctx))) return rc;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    const int chunk = args->stop_on_istop ? 10 : itn;
+    while (done_itn < itn) {
+      const int k = std::min(chunk, itn - done_itn);
+      for (int i = 0; i < k; ++i) {
+        if (graph)
+          CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+        else if ((rc = enqueue_iteration(ctx, ctx->stream)))
+          return rc;
+      }
+      done_itn += k;
+      if (args->stop_on_istop && done_itn < itn) {
+        CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (cur.istop != 0) break;
+      }
+    }
+    CK(cudaEventRecord(ctx->ev1, ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev1));
+    CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  }
+  if (ctx->want_se && done_itn > 0)
+    k_finish_se<<<ctx->gvx, kThreads, 0, ctx->stream>>>(ctx->se, ctx->n, ctx->st, ctx->m_k + ctx->m_d);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
+  std::vector<plsqr_iter> hh((size_t)itn + 1);
+  CK(cudaMemcpyAsync(hh.data(), ctx->hist, sizeof(plsqr_iter) * (itn + 1), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  if (x) CK(cudaMemcpyAsync(x, ctx->x, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+  if (w) CK(cudaMemcpyAsync(w, ctx->w, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+  if (se && ctx->want_se)
+    CK(cudaMemcpyAsync(se, ctx->se, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->solved = true;
+
+  plsqr_result r;
+  memset(&r, 0, sizeof(r));
+  r.istop = (args->damp > 0.0 && cur.istop == 2) ? 3 : cur.istop;  // lsqr.c:895-896
+  r.itn = cur.itn;
+  r.anorm = cur.anorm;
+  r.acond = cur.acond;
+  r.rnorm = cur.rnorm;
+  r.arnorm_out = cur.test2;
+  r.xnorm = cur.xnorm;
+  r.arnorm = cur.arnorm;
+  r.bnorm = cur.bnorm;
+  r.dxmax = cur.dxmax;
+  r.maxdx = cur.maxdx;
+  r.seconds = ms * 1e-3;
+  if (res) *res = r;
+  if (hist) memcpy(hist, hh.data(), sizeof(plsqr_iter) * (itn + 1));
+  if (ctx->opts.verbose) print_iterations(hh.data(), r.itn, r.seconds);
+  if (args->result_txt) {
+    if ((rc = write_result_txt(args->result_txt, ctx->m_k + ctx->m_d, ctx->n, args, hh.data(),
+                               cur.done ? -1 : r.itn, &r)))
+      return rc;
+  }
+  return PLSQR_OK;
+}
+
+int plsqr_get_x(plsqr_ctx *ctx, double *x) {
+  if (!ctx || !x) return PLSQR_ERR_ARG;
+  if (!ctx->solved) return PLSQR_ERR_STATE;
+  CK(cudaSetDevice(ctx->opts.device));
+  CK(cudaMemcpy(x, ctx->x, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+  return PLSQR_OK;
+}
+
+int plsqr_write_result(plsqr_ctx *ctx, const char *path) {
+  if (!ctx || !path) return PLSQR_ERR_ARG;
+  std::vector<double> x((size_t)ctx->n);
+  int rc = plsqr_get_x(ctx, x.data());
+  if (rc) return rc;
+  return plsqr_io_write_x(path, ctx->n, x.data());
+}
+
+}  // extern "C"

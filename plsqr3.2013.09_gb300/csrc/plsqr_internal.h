@@ -1,0 +1,71 @@
+// Internal definitions shared by the device and host sources of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <utility>
+#include <vector>
+
+#include "dev_types.h"
+#include "plsqr_gpu.h"
+
+// One compressed-sparse operand in device memory.
+struct DevLines {
+  int64_t *ptr = nullptr;
+  int32_t *idx = nullptr;
+  double *val = nullptr;
+  int32_t n_lines = 0;
+  int64_t nnz = 0;
+  plsqr::Csr csr() const { return plsqr::Csr{ptr, idx, val, n_lines}; }
+};
+
+struct MixedState;  // mixed.cu
+
+struct plsqr_ctx {
+  plsqr_opts opts;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int32_t m_k = 0, m_d = 0, n = 0;
+  int64_t nnz_k = 0, nnz_d = 0;
+  int sm_count = 0, blocks_per_sm = 0;
+  DevLines K, D, KC, DC;  // kernel/damping by row, kernel/damping by column
+  double *u = nullptr, *v = nullptr, *w = nullptr, *x = nullptr, *se = nullptr, *xref = nullptr;
+  double *parts_u = nullptr, *parts_v = nullptr, *parts_dk = nullptr, *parts_err = nullptr;
+  plsqr::DevState *st = nullptr;
+  plsqr_iter *hist = nullptr;
+  int hist_cap = 0;
+  bool want_se = false, has_ref = false, solved = false;
+  int g1k = 1, g1d = 1, g2 = 1, gvu = 1, gvx = 1, gsk = 1, gsd = 1;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_key = -1;
+  plsqr_iter *graph_hist = nullptr;
+  std::vector<double> b_k;  // right-hand side loaded from the files, if any
+  std::vector<std::pair<void *, size_t>> allocs;
+  int64_t device_bytes = 0;
+  char last_error[512] = {0};
+  MixedState *mixed = nullptr;
+};
+
+void ctx_set_error(plsqr_ctx *ctx, const char *fmt, ...);
+int ctx_dev_alloc_bytes(plsqr_ctx *ctx, void **p, size_t bytes);
+void ctx_dev_free(plsqr_ctx *ctx, void *p);
+
+template <class T>
+inline int dev_alloc(plsqr_ctx *ctx, T **p, size_t count) {
+  void *q = nullptr;
+  const int rc = ctx_dev_alloc_bytes(ctx, &q, (count > 0 ? count : 1) * sizeof(T));
+  *p = (T *)q;
+  return rc;
+}
+inline void dev_free(plsqr_ctx *ctx, void *p) { ctx_dev_free(ctx, p); }
+
+// report.cpp
+int write_result_txt(const char *path, int num_row, int n, const plsqr_lsqr_args *args,
+                     const plsqr_iter *hist, int itn, const plsqr_result *r);
+void print_iterations(const plsqr_iter *hist, int itn, double seconds);
+
+// mixed.cu
+int mixed_prepare(plsqr_ctx *ctx);
+int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, double *x,
+               double *w, double *se, plsqr_iter *hist, plsqr_result *res);
+void mixed_free(plsqr_ctx *ctx);

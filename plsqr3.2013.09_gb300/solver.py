@@ -1,0 +1,162 @@
+"""Python face of the GB300 solver: the reference's aprod / lsqr interface.
+
+`Context` owns one device context of libplsqr_gpu.so.  Its methods mirror
+the reference's operator and driver:
+
+  aprod(mode)          aprod(version, rank, np, mode, m, n, x, y, UsrWrk, ...)
+                       on the device-resident vectors (source/aprod.c:24-84)
+  aprod_host(mode,...) the same on host vectors, updated in place
+  lsqr(...)            lsqr(...) with call_lsqr's constants by default
+                       (source/lsqr.c:34-184, 195-917)
+
+Every call goes through the C ABI; there is no CPU path here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .synth import Problem
+
+
+def _f64(a, n, name):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.shape != (n,):
+        raise ValueError(f"{name} must have {n} values, got shape {a.shape}")
+    return a
+
+
+class Context:
+    def __init__(self, problem: Problem | None = None, *, files: dict | None = None,
+                 precision: str = "fp64", device: int = 0, use_graph: bool = True,
+                 verbose: bool = False):
+        L = N.lib()
+        o = N.Opts()
+        L.plsqr_default_opts(C.byref(o))
+        o.device = device
+        o.precision = N.PREC_MIXED if precision == "mixed" else N.PREC_FP64
+        o.use_graph = int(use_graph)
+        o.verbose = int(verbose)
+        h = N.vp()
+        if files is not None:
+            f = N.Files()
+            for k in ("ker_f", "ker_i", "damp_f", "damp_i", "damp_f_bycol", "damp_i_bycol",
+                      "b_k"):
+                setattr(f, k, str(files[k]).encode())
+            f.dir = str(files["dir"]).encode()
+            f.row_k, f.row_d, f.col = int(files["row_k"]), int(files["row_d"]), int(files["col"])
+            N.check(L.plsqr_ctx_create_files(C.byref(f), C.byref(o), C.byref(h)),
+                    "plsqr_ctx_create_files")
+        else:
+            if problem is None:
+                raise ValueError("a Problem or files is needed")
+            k, d, dc = (problem.k_csc.as_native(), problem.d_csr.as_native(),
+                        problem.d_csc.as_native())
+            N.check(L.plsqr_ctx_create(C.byref(k), C.byref(d), C.byref(dc), C.byref(o),
+                                       C.byref(h)), "plsqr_ctx_create")
+        self._h = h
+        self.precision = precision
+        info = self.info()
+        self.m_k, self.m_d, self.n = info["m_k"], info["m_d"], info["n"]
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().plsqr_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, where):
+        N.check(rc, where, self._h)
+
+    def info(self) -> dict:
+        i = N.Info()
+        self._check(N.lib().plsqr_ctx_info(self._h, C.byref(i)), "plsqr_ctx_info")
+        return {k: getattr(i, k) for k, _ in N.Info._fields_}
+
+    # -- vectors ------------------------------------------------------------
+    def set_u(self, y_k, y_d=None) -> None:
+        yk = _f64(y_k, self.m_k, "y_k")
+        yd = None if y_d is None else _f64(y_d, self.m_d, "y_d")
+        self._check(N.lib().plsqr_set_u(self._h, N.ptr(yk), N.ptr(yd)), "plsqr_set_u")
+
+    def get_u(self):
+        yk, yd = np.empty(self.m_k), np.empty(self.m_d)
+        self._check(N.lib().plsqr_get_u(self._h, N.ptr(yk), N.ptr(yd)), "plsqr_get_u")
+        return yk, yd
+
+    def set_v(self, v) -> None:
+        vv = _f64(v, self.n, "v")
+        self._check(N.lib().plsqr_set_v(self._h, N.ptr(vv)), "plsqr_set_v")
+
+    def get_v(self):
+        v = np.empty(self.n)
+        self._check(N.lib().plsqr_get_v(self._h, N.ptr(v)), "plsqr_get_v")
+        return v
+
+    def get_b(self):
+        b = np.empty(self.m_k)
+        self._check(N.lib().plsqr_get_b(self._h, N.ptr(b)), "plsqr_get_b")
+        return b
+
+    # -- operator -----------------------------------------------------------
+    def aprod(self, mode: int, iteration: int = 1, is_final: int = 0) -> None:
+        self._check(N.lib().plsqr_aprod(self._h, mode, iteration, is_final), "plsqr_aprod")
+
+    def aprod_host(self, mode: int, y_k: np.ndarray, y_d: np.ndarray, x: np.ndarray,
+                   iteration: int = 1, is_final: int = 0) -> None:
+        for a, n, nm in ((y_k, self.m_k, "y_k"), (y_d, self.m_d, "y_d"), (x, self.n, "x")):
+            if a.dtype != np.float64 or a.shape != (n,) or not a.flags.c_contiguous:
+                raise ValueError(f"{nm} must be a contiguous float64 array of {n} values")
+        self._check(N.lib().plsqr_aprod_host(self._h, mode, N.ptr(y_k), N.ptr(y_d), N.ptr(x),
+                                             iteration, is_final), "plsqr_aprod_host")
+
+    # -- driver -------------------------------------------------------------
+    def set_reference_x(self, x_ref) -> None:
+        xr = None if x_ref is None else _f64(x_ref, self.n, "x_ref")
+        self._check(N.lib().plsqr_set_reference_x(self._h, N.ptr(xr)), "plsqr_set_reference_x")
+
+    def lsqr(self, b_k=None, *, lsqr_iteration: int = 100, damp: float = 0.0,
+             atol: float = 1e-10, btol: float = 1e-10, conlim: float = 100.0,
+             itnlim: int = 1000, want_se: bool = False, stop_on_istop: bool = False,
+             result_txt: str | None = None, sweeps: int = 4, inner: int = 50,
+             want_w: bool = False) -> dict:
+        a = N.LsqrArgs()
+        N.lib().plsqr_default_lsqr_args(C.byref(a))
+        a.damp, a.atol, a.btol, a.conlim = damp, atol, btol, conlim
+        a.itnlim, a.lsqr_iteration = itnlim, lsqr_iteration
+        a.want_se, a.stop_on_istop = int(want_se), int(stop_on_istop)
+        a.result_txt = result_txt.encode() if result_txt else None
+        a.sweeps, a.inner = sweeps, inner
+        b = None if b_k is None else _f64(b_k, self.m_k, "b_k")
+        n_hist = (sweeps * inner if self.precision == "mixed" else lsqr_iteration) + 1
+        x = np.empty(self.n)
+        w = np.empty(self.n) if want_w else None
+        se = np.empty(self.n) if want_se else None
+        hist = np.zeros(n_hist, N.ITER_DTYPE)
+        r = N.Result()
+        self._check(N.lib().plsqr_lsqr(self._h, C.byref(a), N.ptr(b), N.ptr(x), N.ptr(w),
+                                       N.ptr(se), N.ptr(hist), C.byref(r)), "plsqr_lsqr")
+        res = {k: getattr(r, k) for k, _ in N.Result._fields_ if k != "pad"}
+        return dict(x=x, w=w, se=se, hist=hist, result=res)
+
+    def get_x(self):
+        x = np.empty(self.n)
+        self._check(N.lib().plsqr_get_x(self._h, N.ptr(x)), "plsqr_get_x")
+        return x
+
+    def write_result(self, path: str) -> None:
+        self._check(N.lib().plsqr_write_result(self._h, str(path).encode()), "plsqr_write_result")
