@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 PLSQR3 hot path: the LSQR iteration and its aprod.
+
+Workload: the 96x96x32-cell tomography problem (294,912 columns, 200,000 rays
+of radius-6 tubes, ~1.33e9 kernel nonzeros, 1,148,928 damping rows), plain
+FP64 LSQR for 300 iterations.  One step = one LSQR solve with the matrix
+resident in HBM.
+
+  value  = algorithmic HBM bytes of the solve's main loop / its device time
+           (CUDA events on the solver's stream around the iteration loop)
+  e2e    = the same bytes / wall time of the whole plsqr_lsqr call with host
+           b_k in and host x out (H2D and D2H inside the timed region)
+
+Extra keys: roofline of the dominant kernel (mode-2 product), the CPU
+baseline (the oracle port, FP64, all host threads, bounded sample), the
+time to 1e-6 relative error vs the FP64 solution for plain FP64 and mixed
+precision, clocks sampled during the timed region.
+
+`--impl reference` times the reference CPU implementation of the same solve
+(the oracle port of source/lsqr.c + aprod_impl.c + CPUSpMV.c, OpenMP on all
+host cores) on a bounded sample and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import __graft_entry__ as graft  # noqa: E402
+
+METRIC = "aprod HBM GB/s (plain FP64 LSQR iteration)"
+UNIT = "GB/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "aprod_fp64_grid96.md"
+    if not p.exists():
+        return None
+    m = re.search(rf"^{kernel}_dram_bytes_per_launch:\s*([0-9.eE+]+)", p.read_text(), re.M)
+    return float(m.group(1)) if m else None
+
+
+class Clocks:
+    """nvidia-smi sampling (every 200 ms) during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample(pkg, orc, prob, iterations: int) -> dict:
+    """The oracle port (FP64, OpenMP on every host thread) timed on a few
+    LSQR iterations of the same problem; GB/s of the same algorithmic bytes."""
+    o = orc.OracleProblem(prob)
+    threads = orc.get_threads()
+    t0 = time.perf_counter()
+    o.lsqr(iterations)
+    dt = time.perf_counter() - t0
+    return dict(seconds=dt, iterations=iterations, threads=threads)
+
+
+def max_over_ranks(values: list[float]) -> list[float]:
+    """Element-wise maximum over the ranks of an initialised process group
+    (the replicas' times); the values themselves on a single process."""
+    try:
+        import torch.distributed as tdist
+        if not (tdist.is_available() and tdist.is_initialized()):
+            return list(values)
+        import torch
+    except ImportError:
+        return list(values)
+    t = torch.tensor(values, dtype=torch.float64)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def first_below(err: np.ndarray, tol: float):
+    idx = np.nonzero((err >= 0) & (err <= tol))[0]
+    return int(idx[0]) if idx.size else None
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="grid96")
+    ap.add_argument("--iterations", type=int, default=None)
+    ap.add_argument("--cpu-iterations", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tts", action="store_true", help="skip the time-to-1e-6 runs")
+    ap.add_argument("--profile", action="store_true",
+                    help="profiling run: build the context, run one short solve, exit")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    args = ap.parse_args()
+
+    ws, rank, local = dist()
+    pkg = graft.load_package()
+    cfg = pkg.CONFIGS[args.config]
+    iters = args.iterations or cfg["iterations"]
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        orc = graft.load_oracle()
+        log(f"generating {args.config} ...")
+        prob = pkg.generate(args.config)
+        bytes_it = algorithmic_bytes(prob)
+        per = []
+        for _ in range(args.warmup if args.warmup < 1 else 1):
+            cpu_sample(pkg, orc, prob, 1)
+        for _ in range(args.steps):
+            s = cpu_sample(pkg, orc, prob, args.cpu_iterations)
+            per.append(s)
+        secs = sum(s["seconds"] for s in per)
+        its = sum(s["iterations"] for s in per)
+        value = bytes_it * its / secs / 1e9
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+                "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded generator, reference file formats)",
+                "config": workload(args.config, prob, iters),
+                "cpu_baseline": {"value": value, "unit": UNIT, "cores": per[0]["threads"],
+                                 "kind": "port",
+                                 "sample": f"{args.cpu_iterations} LSQR iterations (plus start-up) "
+                                           f"per step of the {args.config} solve"},
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    if args.profile:
+        prob = pkg.generate(args.config)
+        with pkg.Context(prob, device=local, precision=args.precision) as ctx:
+            if args.precision == "mixed":
+                out = ctx.lsqr(sweeps=1, inner=iters)
+            else:
+                out = ctx.lsqr(lsqr_iteration=iters)
+        log(f"profile run: {args.config}, {iters} iterations, "
+            f"{out['result']['seconds'] * 1e3:.2f} ms")
+        return 0
+
+    # ---- GB300 arm ----------------------------------------------------------
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("gloo")
+    log(f"[rank {rank}] generating {args.config} ...")
+    t0 = time.perf_counter()
+    prob = pkg.generate(args.config)
+    log(f"[rank {rank}] generated in {time.perf_counter() - t0:.1f}s: m_k={prob.m_k} "
+        f"m_d={prob.m_d} n={prob.n} nnz_k={prob.meta['nnz_k']}")
+    t0 = time.perf_counter()
+    ctx = pkg.Context(prob, device=local)
+    info = ctx.info()
+    log(f"[rank {rank}] context in {time.perf_counter() - t0:.1f}s, "
+        f"{info['device_bytes'] / 1e9:.1f} GB on device")
+    bytes_it = info["hbm_bytes_iteration"]
+    b = np.ascontiguousarray(prob.b_k)
+
+    for _ in range(args.warmup):
+        ctx.lsqr(b, lsqr_iteration=iters)
+    if ws > 1:
+        tdist.barrier()
+    dev_s, wall = 0.0, 0.0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            out = ctx.lsqr(b, lsqr_iteration=iters)  # host b in, host x out
+            wall += time.perf_counter() - t
+            dev_s += out["result"]["seconds"]
+    dev_s, wall = max_over_ranks([dev_s, wall])
+    clocks = clk.summary()
+    value = ws * bytes_it * iters * args.steps / dev_s / 1e9
+    e2e = ws * bytes_it * iters * args.steps / wall / 1e9
+
+    # dominant kernel: time each product kernel alone (events on its stream)
+    ms1 = ctx.bench_aprod(1, reps=10)
+    ms2 = ctx.bench_aprod(2, reps=10)
+    ms_it = ctx.bench_iteration(reps=20)
+    dom_mode = 2 if ms2 >= ms1 else 1
+    ms_dom = ms2 if dom_mode == 2 else ms1
+    bytes_dom = info[f"hbm_bytes_aprod{dom_mode}"]
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_dom / (ms_dom * 1e-3) / 1e9
+    kname = "k_aprod2" if dom_mode == 2 else "k_aprod1"
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": ncu_traffic(kname),
+                "kernel": kname, "peak_kind": peak_kind,
+                "ms_per_launch": {"k_aprod1": ms1, "k_aprod2": ms2, "iteration": ms_it},
+                "bytes_per_launch": bytes_dom}
+
+    extra = {}
+    if not args.no_tts and rank == 0:
+        extra["time_to_1e-6"] = time_to_tol(pkg, prob, ctx, iters, 1e-6)
+    ctx.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        orc = graft.load_oracle()
+        s = cpu_sample(pkg, orc, prob, args.cpu_iterations)
+        cpu = {"value": bytes_it * s["iterations"] / s["seconds"] / 1e9, "unit": UNIT,
+               "cores": s["threads"], "kind": "port",
+               "sample": f"{s['iterations']} LSQR iterations (plus start-up) of the same solve, "
+                         f"{s['seconds']:.1f} s"}
+    if rank != 0:
+        return 0
+    launches = (4 + 5 * iters) * args.steps
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generator, reference file formats)",
+            "config": workload(args.config, prob, iters),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * prob.m_k,
+                    "d2h_bytes_per_step": 8 * prob.n + 96 * (iters + 1) + 96},
+            "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clocks, **extra}
+    print(json.dumps(line))
+    return 0
+
+
+def algorithmic_bytes(prob) -> float:
+    """Bytes of one LSQR iteration, as plsqr_ctx_info computes them."""
+    nk, nd = prob.meta["nnz_k"], prob.meta["nnz_d"]
+    mk, md, n = prob.m_k, prob.m_d, prob.n
+    a1 = 12.0 * (nk + nd) + 8.0 * (mk + 1 + md + 1) + 16.0 * (mk + md) + 8.0 * n
+    a2 = 12.0 * (nk + nd) + 16.0 * (n + 1) + 16.0 * n + 8.0 * (mk + md)
+    return a1 + a2 + 16.0 * (mk + md) + 8.0 * 6 * n
+
+
+def workload(name, prob, iters) -> dict:
+    return {"workload": f"{name}: FP64 LSQR, {iters} iterations, grid "
+                        f"{'x'.join(map(str, prob.meta['grid']))}, {prob.m_k} rays "
+                        f"(tube radius {prob.meta['tube_radius']})",
+            "m_k": prob.m_k, "m_d": prob.m_d, "n": prob.n, "nnz_k": prob.meta["nnz_k"],
+            "nnz_d": prob.meta["nnz_d"], "iterations": iters,
+            "l2": "inputs larger than L2 (kernel matrix ~32 GB per iteration)"}
+
+
+def time_to_tol(pkg, prob, ctx64, iters, tol) -> dict:
+    """Time to reach ||x - x*|| / ||x*|| <= tol, x* = FP64 LSQR run to twice
+    the iteration count; plain FP64 vs mixed precision."""
+    xstar = ctx64.lsqr(lsqr_iteration=2 * iters)["x"]
+    ctx64.set_reference_x(xstar)
+    h = ctx64.lsqr(lsqr_iteration=2 * iters)["hist"]
+    k64 = first_below(h["err"], tol)
+    ctx64.set_reference_x(None)
+    out = {"tol": tol, "reference": f"FP64 LSQR, {2 * iters} iterations"}
+    if k64 is not None:
+        t = [ctx64.lsqr(lsqr_iteration=k64)["result"]["seconds"] for _ in range(3)]
+        out["fp64"] = {"iterations": k64, "seconds": min(t)}
+    else:
+        out["fp64"] = {"iterations": None, "final_err": float(h["err"][-1])}
+    with pkg.Context(prob, precision="mixed") as cm:
+        cm.set_reference_x(xstar)
+        best = None
+        for sweeps, inner in ((3, 50), (4, 50), (5, 50), (6, 50)):
+            hm = cm.lsqr(sweeps=sweeps, inner=inner)["hist"]
+            k = first_below(hm["err"], tol)
+            if k is not None:
+                best = (sweeps, inner, k)
+                break
+        cm.set_reference_x(None)
+        if best:
+            s, i, k = best
+            need = (k - 1) // i + 1  # sweeps until the crossing
+            t = [cm.lsqr(sweeps=need, inner=i)["result"]["seconds"] for _ in range(3)]
+            out["mixed"] = {"sweeps": need, "inner": i, "inner_iterations_to_tol": k,
+                            "seconds": min(t)}
+            if "seconds" in out["fp64"]:
+                out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds"] / min(t)
+        else:
+            out["mixed"] = {"sweeps": None, "final_err": float(hm["err"][-1])}
+    return out
+
+
+if __name__ == "__main__":
+    sys.exit(main())

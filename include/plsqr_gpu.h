@@ -79,6 +79,12 @@ typedef struct {
   int32_t precision; /* PLSQR_PREC_*                                          */
   int32_t use_graph; /* capture each LSQR iteration as a CUDA graph (def. 1)  */
   int32_t verbose;   /* print the per-iteration alpha/beta lines like lsqr.c  */
+  /* Optional model grid (nx, ny, nz) with column = (iz*ny + iy)*nx + ix, the
+   * cell map of damping_binary.py; when given (and nx*ny*nz = n) the A^T y
+   * product visits the columns in 3-D Morton order so that cells sharing
+   * rays are gathered together.  Zeros: natural column order. */
+  int32_t grid[3];
+  int32_t pad;
 } plsqr_opts;
 
 typedef struct {
@@ -186,6 +192,16 @@ int plsqr_set_reference_x(plsqr_ctx *ctx, const double *x_ref);
 int plsqr_get_x(plsqr_ctx *ctx, double *x);
 /* mpiio_write_result (source/plsqr3.c:1986-2013): raw FP64 x[n]. */
 int plsqr_write_result(plsqr_ctx *ctx, const char *path);
+
+/* ---- measurement (no counterpart in the reference) ---------------------- */
+/* Average device time of one launch of the mode-1 or mode-2 product kernel
+ * (y += A x or x += A^T y on the context's vectors, which it overwrites),
+ * from CUDA events around `reps` back-to-back launches on the context's
+ * stream. */
+int plsqr_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch);
+/* The same for one LSQR iteration replayed from its CUDA graph; needs a
+ * preceding plsqr_lsqr on the context (state and history are overwritten). */
+int plsqr_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration);
 
 /* ---- files, host side (no GPU needed) ----------------------------------- */
 /* read_kernel_col_info (plsqr3.c:1379-1409): nnz[n], start[n] (0-based,

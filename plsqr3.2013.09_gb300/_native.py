@@ -39,7 +39,8 @@ class Files(C.Structure):
 
 
 class Opts(C.Structure):
-    _fields_ = [("device", i32), ("precision", i32), ("use_graph", i32), ("verbose", i32)]
+    _fields_ = [("device", i32), ("precision", i32), ("use_graph", i32), ("verbose", i32),
+                ("grid", i32 * 3), ("pad", i32)]
 
 
 class Info(C.Structure):
@@ -95,6 +96,8 @@ SIGNATURES = {
     "plsqr_set_reference_x": (C.c_int, [vp, vp]),
     "plsqr_get_x": (C.c_int, [vp, vp]),
     "plsqr_write_result": (C.c_int, [vp, C.c_char_p]),
+    "plsqr_bench_aprod": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(f64)]),
+    "plsqr_bench_iteration": (C.c_int, [vp, C.c_int, C.POINTER(f64)]),
     "plsqr_io_read_kernel_info": (C.c_int, [C.c_char_p, i32, vp, vp, C.POINTER(i64)]),
     "plsqr_io_read_kernel": (C.c_int, [C.c_char_p, C.c_char_p, i32, i32, vp, vp, vp]),
     "plsqr_io_read_int32_counts": (C.c_int, [C.c_char_p, i64, vp, C.POINTER(i64)]),

@@ -23,9 +23,11 @@
 
 namespace plsqr {
 
-// Sum of val[e] * x[idx[e]] over [beg, end) by one warp; the result is valid
-// in every lane.
-__device__ __forceinline__ double warp_dot_f64(const int32_t *__restrict__ idx,
+// This lane's share of sum val[e] * x[idx[e]] over [beg, end) when one warp
+// streams the range: 16-byte loads of 4 indices and 2x2 values per lane and
+// step, kUnroll steps in flight.  Reduce across the warp with warp_sum.
+template <int kUnroll>
+__device__ __forceinline__ double lane_dot_f64(const int32_t *__restrict__ idx,
                                                const double *__restrict__ val,
                                                const double *__restrict__ x, int64_t beg,
                                                int64_t end, int lane) {
@@ -35,25 +37,28 @@ __device__ __forceinline__ double warp_dot_f64(const int32_t *__restrict__ idx,
   if (a4 > end) a4 = end;
   if (beg + lane < a4) acc0 = val[beg + lane] * x[idx[beg + lane]];
   const int64_t e4 = a4 + ((end - a4) & ~int64_t(3));
-  // body: groups of 4 aligned elements, lane-strided; two groups in flight
   const int4 *__restrict__ idx4 = reinterpret_cast<const int4 *>(idx);
   const double2 *__restrict__ val2 = reinterpret_cast<const double2 *>(val);
   int64_t g = (a4 >> 2) + lane;
   const int64_t gend = e4 >> 2;
-  for (; g + 32 < gend; g += 64) {
-    const int4 c0 = __ldg(idx4 + g), c1 = __ldg(idx4 + g + 32);
-    const double2 v0 = __ldg(val2 + 2 * g), v1 = __ldg(val2 + 2 * g + 1);
-    const double2 w0 = __ldg(val2 + 2 * (g + 32)), w1 = __ldg(val2 + 2 * (g + 32) + 1);
-    acc0 = fma(v0.x, __ldg(x + c0.x), acc0);
-    acc1 = fma(v0.y, __ldg(x + c0.y), acc1);
-    acc0 = fma(v1.x, __ldg(x + c0.z), acc0);
-    acc1 = fma(v1.y, __ldg(x + c0.w), acc1);
-    acc0 = fma(w0.x, __ldg(x + c1.x), acc0);
-    acc1 = fma(w0.y, __ldg(x + c1.y), acc1);
-    acc0 = fma(w1.x, __ldg(x + c1.z), acc0);
-    acc1 = fma(w1.y, __ldg(x + c1.w), acc1);
+  for (; g + 32 * (kUnroll - 1) < gend; g += 32 * kUnroll) {
+    int4 c[kUnroll];
+    double2 v0[kUnroll], v1[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      c[u] = __ldg(idx4 + g + 32 * u);
+      v0[u] = __ldg(val2 + 2 * (g + 32 * u));
+      v1[u] = __ldg(val2 + 2 * (g + 32 * u) + 1);
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      acc0 = fma(v0[u].x, __ldg(x + c[u].x), acc0);
+      acc1 = fma(v0[u].y, __ldg(x + c[u].y), acc1);
+      acc0 = fma(v1[u].x, __ldg(x + c[u].z), acc0);
+      acc1 = fma(v1[u].y, __ldg(x + c[u].w), acc1);
+    }
   }
-  if (g < gend) {
+  for (; g < gend; g += 32) {
     const int4 c0 = __ldg(idx4 + g);
     const double2 v0 = __ldg(val2 + 2 * g), v1 = __ldg(val2 + 2 * g + 1);
     acc0 = fma(v0.x, __ldg(x + c0.x), acc0);
@@ -63,10 +68,21 @@ __device__ __forceinline__ double warp_dot_f64(const int32_t *__restrict__ idx,
   }
   // tail: up to 3 elements
   if (e4 + lane < end) acc1 = fma(val[e4 + lane], x[idx[e4 + lane]], acc1);
-  double s = acc0 + acc1;
+  return acc0 + acc1;
+}
+
+__device__ __forceinline__ double warp_sum(double s) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
+}
+
+// Sum of val[e] * x[idx[e]] over [beg, end) by one warp; valid in every lane.
+__device__ __forceinline__ double warp_dot_f64(const int32_t *__restrict__ idx,
+                                               const double *__restrict__ val,
+                                               const double *__restrict__ x, int64_t beg,
+                                               int64_t end, int lane) {
+  return warp_sum(lane_dot_f64<2>(idx, val, x, beg, end, lane));
 }
 
 // Sequential sum in stored order, mul and add rounded separately.
@@ -116,21 +132,25 @@ enum ScaleMode : int {
 // ---------------------------------------------------------------------------
 // M1: u_k[r] = s*u_k[r] + (K v)[r], u_d[r] = s*u_d[r] + (D v)[r]; per-block
 // partial sums of squares of the new u: parts[0..gk) kernel rows,
-// parts[gk..gk+gd) damping rows.
-template <int kThreads>
+// parts[gk..gk+gd) damping rows.  Warp w of the kernel blocks owns rows
+// [kpart[w], kpart[w+1]), a contiguous range holding about the same number of
+// nonzeros as every other warp's.
+template <int kThreads, int kUnroll>
 __global__ void __launch_bounds__(kThreads)
-    k_aprod1(Csr K, Csr D, const double *__restrict__ v, double *__restrict__ u, int gk,
-             int mode, const DevState *__restrict__ st, double *__restrict__ parts) {
+    k_aprod1(Csr K, Csr D, const int32_t *__restrict__ kpart, const double *__restrict__ v,
+             double *__restrict__ u, int gk, int mode, const DevState *__restrict__ st,
+             double *__restrict__ parts) {
   __shared__ double smem[kThreads / 32];
   double s = 1.0;
   if (mode == kScaleNegAlpha) s = -st->alpha;
   double sq = 0.0;
   if ((int)blockIdx.x < gk) {
     const int lane = threadIdx.x & 31;
-    const int warps_total = gk * (kThreads / 32);
-    for (int r = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); r < K.n_lines;
-         r += warps_total) {
-      const double t = warp_dot_f64(K.idx, K.val, v, K.ptr[r], K.ptr[r + 1], lane);
+    const int w = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+    const int r1 = kpart[w + 1];
+    for (int r = kpart[w]; r < r1; ++r) {
+      const double t =
+          warp_sum(lane_dot_f64<kUnroll>(K.idx, K.val, v, K.ptr[r], K.ptr[r + 1], lane));
       if (lane == 0) {
         const double y = dadd(dmul(s, u[r]), t);  // dscal, then y_k += t_k
         u[r] = y;
@@ -185,13 +205,20 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---------------------------------------------------------------------------
-// M2: v[c] = s*v[c] + ((K^T u_k)[c] + (D^T u_d)[c]); per-block partial sum of
-// squares of the new v.  In LSQR mode the whole kernel is skipped when
-// beta == 0 (source/lsqr.c:530).
-template <int kThreads>
+// M2: v[c] = s*v[c] + (K^T u_k + D^T u_d)[c]; per-block partial sum of
+// squares of the new v.  The columns are visited in the order corder (the
+// natural order, or 3-D Morton order of the cells); block b owns the visit
+// positions [cpart[b], cpart[b+1]) (balanced by nonzeros) and its warps take
+// them in turn, so that neighbouring cells, which share most of their rays,
+// are gathered at the same time on the same SM and reuse u_k from L1.  A column's kernel entries
+// are streamed by the whole warp and its damping entries (a few per column)
+// are spread over the lanes, so every FP64 instruction runs on a full warp.
+// In LSQR mode the kernel is skipped when beta == 0 (source/lsqr.c:530).
+template <int kThreads, int kUnroll>
 __global__ void __launch_bounds__(kThreads)
-    k_aprod2(Csr KC, Csr DC, const double *__restrict__ u, int m_k, double *__restrict__ v,
-             int mode, const DevState *__restrict__ st, double *__restrict__ parts) {
+    k_aprod2(Csr KC, Csr DC, const int32_t *__restrict__ cpart, const int32_t *__restrict__ corder,
+             const double *__restrict__ u, int m_k, double *__restrict__ v, int mode,
+             const DevState *__restrict__ st, double *__restrict__ parts) {
   __shared__ double smem[kThreads / 32];
   double s = 1.0;
   if (mode == kScaleNegBeta) {
@@ -203,14 +230,16 @@ __global__ void __launch_bounds__(kThreads)
   }
   const double *ud = u + m_k;
   const int lane = threadIdx.x & 31;
-  const int warps_total = gridDim.x * (kThreads / 32);
+  const int c1 = cpart[blockIdx.x + 1];
   double sq = 0.0;
-  for (int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); c < KC.n_lines;
-       c += warps_total) {
-    const double sk = warp_dot_f64(KC.idx, KC.val, u, KC.ptr[c], KC.ptr[c + 1], lane);
+  for (int k = cpart[blockIdx.x] + (threadIdx.x >> 5); k < c1; k += kThreads / 32) {
+    const int c = corder[k];
+    double acc = lane_dot_f64<kUnroll>(KC.idx, KC.val, u, KC.ptr[c], KC.ptr[c + 1], lane);
+    for (int64_t e = DC.ptr[c] + lane; e < DC.ptr[c + 1]; e += 32)
+      acc = fma(DC.val[e], ud[DC.idx[e]], acc);
+    const double t = warp_sum(acc);
     if (lane == 0) {
-      const double sd = seq_dot_f64(DC.idx, DC.val, ud, DC.ptr[c], DC.ptr[c + 1]);
-      const double y = dadd(dmul(s, v[c]), dadd(sk, sd));  // x += (s_k + s_d)
+      const double y = dadd(dmul(s, v[c]), t);  // x += (s_k + s_d)
       v[c] = y;
       sq = fma(y, y, sq);
     }

@@ -229,3 +229,62 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   if (hist) memcpy(hist, hh.data(), sizeof(plsqr_iter) * (total + 1));
   return PLSQR_OK;
 }
+
+int mixed_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch) {
+  int rc;
+  if ((rc = mixed_prepare(ctx))) return rc;
+  MixedState *M = ctx->mixed;
+  CK(cudaSetDevice(ctx->opts.device));
+  auto launch = [&]() {
+    if (mode == 1)
+      k_aprod1_f32<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, ctx->stream>>>(
+          rows_f(ctx), ctx->D.csr(), M->vf, M->uf, ctx->g1k, ctx->st, ctx->parts_u);
+    else
+      k_aprod2_f32<kThreads><<<ctx->g2, kThreads, 0, ctx->stream>>>(
+          cols_f(ctx), ctx->DC.csr(), M->uf, ctx->m_k, M->vf, 1, ctx->st, ctx->parts_v);
+  };
+  // a state with beta > 0 and alpha = 0 so that both kernels run fully
+  DevState h;
+  memset(&h, 0, sizeof(h));
+  h.s_beta_pos = 1;
+  h.beta = 1.0;
+  CK(cudaMemcpy(ctx->st, &h, sizeof(h), cudaMemcpyHostToDevice));
+  launch();
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int i = 0; i < reps; ++i) launch();
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaGetLastError());
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *ms_per_launch = (double)ms / reps;
+  return PLSQR_OK;
+}
+
+int mixed_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration) {
+  if (!ctx->solved || !ctx->mixed) return PLSQR_ERR_STATE;
+  CK(cudaSetDevice(ctx->opts.device));
+  int rc;
+  if (ctx->hist_cap < reps + 1) {
+    dev_free(ctx, ctx->hist);
+    ctx->hist = nullptr;
+    ctx->hist_cap = 0;
+    if ((rc = dev_alloc(ctx, &ctx->hist, (size_t)reps + 1))) return rc;
+    ctx->hist_cap = reps + 1;
+  }
+  if ((rc = ensure_inner_graph(ctx))) return rc;
+  DevState h;
+  CK(cudaMemcpy(&h, ctx->st, sizeof(h), cudaMemcpyDeviceToHost));
+  h.itn = 0;
+  h.hist_base = 0;
+  CK(cudaMemcpy(ctx->st, &h, sizeof(h), cudaMemcpyHostToDevice));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int i = 0; i < reps; ++i) CK(cudaGraphLaunch(ctx->mixed->graph, ctx->stream));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *ms_per_iteration = (double)ms / reps;
+  return PLSQR_OK;
+}

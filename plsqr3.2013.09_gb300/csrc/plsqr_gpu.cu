@@ -156,20 +156,126 @@ static int build_kernel_rows(plsqr_ctx *ctx) {
   return total == ctx->nnz_k ? PLSQR_OK : PLSQR_ERR_INTERNAL;
 }
 
-static void plan_launch(plsqr_ctx *ctx) {
+// Contiguous line ranges [part[w], part[w+1]) with about nnz/parts nonzeros
+// each (a line is never split): the static, balanced warp-to-line map of the
+// product kernels.
+static void balanced_partition(const int64_t *ptr, int32_t n_lines, int parts,
+                               std::vector<int32_t> &out) {
+  out.assign((size_t)parts + 1, 0);
+  const int64_t nnz = ptr[n_lines];
+  for (int w = 1; w < parts; ++w) {
+    const int64_t target = (int64_t)((long double)nnz * w / parts);
+    const int64_t *it = std::lower_bound(ptr, ptr + n_lines + 1, target);
+    int32_t r = (int32_t)(it - ptr);
+    if (r > n_lines) r = n_lines;
+    out[(size_t)w] = std::max(r, out[(size_t)w - 1]);
+  }
+  out[(size_t)parts] = n_lines;
+}
+
+template <int U>
+static void launch_m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  k_aprod1<kThreads, U><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
+      ctx->K.csr(), ctx->D.csr(), ctx->kpart, ctx->v, ctx->u, ctx->g1k, mode, ctx->st, parts);
+}
+template <int U>
+static void launch_m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  k_aprod2<kThreads, U><<<ctx->g2, kThreads, 0, s>>>(ctx->KC.csr(), ctx->DC.csr(), ctx->cpart,
+                                                      ctx->corder, ctx->u, ctx->m_k, ctx->v, mode,
+                                                      ctx->st, parts);
+}
+static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  switch (ctx->unroll) {
+    case 1: launch_m1<1>(ctx, s, mode, parts); break;
+    case 4: launch_m1<4>(ctx, s, mode, parts); break;
+    default: launch_m1<2>(ctx, s, mode, parts);
+  }
+}
+static void m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  switch (ctx->unroll) {
+    case 1: launch_m2<1>(ctx, s, mode, parts); break;
+    case 4: launch_m2<4>(ctx, s, mode, parts); break;
+    default: launch_m2<2>(ctx, s, mode, parts);
+  }
+}
+
+// Spread the low 10 bits of v to every third bit.
+static uint32_t part1by2(uint32_t v) {
+  v &= 0x3ff;
+  v = (v | (v << 16)) & 0x030000ff;
+  v = (v | (v << 8)) & 0x0300f00f;
+  v = (v | (v << 4)) & 0x030c30c3;
+  v = (v | (v << 2)) & 0x09249249;
+  return v;
+}
+
+// Visit order of the columns for the A^T y product: 3-D Morton order of the
+// cells when the grid is known, the natural order otherwise.
+static void column_order(const plsqr_ctx *ctx, std::vector<int32_t> &order) {
+  const int n = ctx->n;
+  order.resize((size_t)n);
+  for (int c = 0; c < n; ++c) order[(size_t)c] = c;
+  const int nx = ctx->opts.grid[0], ny = ctx->opts.grid[1], nz = ctx->opts.grid[2];
+  if (nx <= 0 || ny <= 0 || nz <= 0 || (int64_t)nx * ny * nz != n || nx > 1024 || ny > 1024 ||
+      nz > 1024)
+    return;
+  std::vector<uint32_t> key((size_t)n);
+  for (int c = 0; c < n; ++c) {
+    const uint32_t ix = c % nx, iy = (c / nx) % ny, iz = c / (nx * ny);
+    key[(size_t)c] = part1by2(ix) | (part1by2(iy) << 1) | (part1by2(iz) << 2);
+  }
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return key[(size_t)a] < key[(size_t)b]; });
+}
+
+static int plan_launch(plsqr_ctx *ctx, const std::vector<int64_t> &kc_ptr) {
   const int sm = ctx->sm_count;
   const int wpb = kThreads / 32;
-  // mode 1: warps over kernel rows, threads over damping rows
-  ctx->g1k = std::max(1, std::min(sm * ctx->blocks_per_sm, (ctx->m_k + wpb - 1) / wpb));
-  ctx->g1d = std::max(1, std::min(sm * 2, (ctx->m_d + kThreads - 1) / kThreads));
-  // mode 2: warps over columns
-  ctx->g2 = std::max(1, std::min(sm * ctx->blocks_per_sm, (ctx->n + wpb - 1) / wpb));
+  int occ1 = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_aprod1<kThreads, 2>, kThreads, 0));
+  occ1 = std::max(1, std::min(occ1, ctx->blocks_per_sm));
+  // every reduction kernel writes one partial per block: at most kMaxParts
+  const int half = kMaxParts / 2;
+  // mode 1: one resident wave of warps over kernel rows, threads over damping rows
+  ctx->g1k = std::max(1, std::min({sm * occ1, (ctx->m_k + wpb - 1) / wpb, half}));
+  ctx->g1d = std::max(1, std::min({sm, (ctx->m_d + kThreads - 1) / kThreads, half}));
+  // mode 2: many small blocks of neighbouring columns (several waves)
+  int m2b = ctx->m2_blocks_per_sm;
+  if (const char *e = getenv("PLSQR_M2_BLOCKS_PER_SM"))
+    if (atoi(e) > 0) m2b = atoi(e);
+  ctx->g2 = std::max(1, std::min({sm * m2b, (ctx->n + wpb - 1) / wpb, kMaxParts}));
   // vector kernels
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   ctx->gvu = (int)std::max<int64_t>(1, std::min<int64_t>(sm * 4, (m + kThreads - 1) / kThreads));
   ctx->gvx = std::max(1, std::min(sm * 4, (ctx->n + kThreads - 1) / kThreads));
   ctx->gsk = std::max(1, std::min(sm, (ctx->m_k + kThreads - 1) / kThreads));
   ctx->gsd = std::max(1, std::min(sm, (ctx->m_d + kThreads - 1) / kThreads));
+  // balanced warp ranges over kernel rows (pointer array copied back from
+  // the device transpose) and over columns
+  std::vector<int64_t> krp((size_t)ctx->m_k + 1);
+  CK(cudaMemcpy(krp.data(), ctx->K.ptr, krp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  std::vector<int32_t> kp, cp;
+  balanced_partition(krp.data(), ctx->m_k, ctx->g1k * wpb, kp);
+  std::vector<int32_t> order;
+  column_order(ctx, order);
+  const char *no = getenv("PLSQR_NATURAL_ORDER");
+  if (no && atoi(no) > 0)
+    for (int c = 0; c < ctx->n; ++c) order[(size_t)c] = c;
+  std::vector<int64_t> optr((size_t)ctx->n + 1);  // nonzero prefix in visit order
+  optr[0] = 0;
+  for (int k = 0; k < ctx->n; ++k) {
+    const int c = order[(size_t)k];
+    optr[(size_t)k + 1] = optr[(size_t)k] + (kc_ptr[(size_t)c + 1] - kc_ptr[(size_t)c]);
+  }
+  balanced_partition(optr.data(), ctx->n, ctx->g2, cp);  // per block
+  int rc;
+  if ((rc = dev_alloc(ctx, &ctx->kpart, kp.size())) || (rc = dev_alloc(ctx, &ctx->cpart, cp.size())) ||
+      (rc = dev_alloc(ctx, &ctx->corder, order.size())))
+    return rc;
+  CK(cudaMemcpy(ctx->corder, order.data(), order.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->kpart, kp.data(), kp.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->cpart, cp.data(), cp.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  return PLSQR_OK;
 }
 
 static void free_graph(plsqr_ctx *ctx) {
@@ -188,6 +294,10 @@ static int ctx_init_common(plsqr_ctx *ctx) {
   if (ctx->blocks_per_sm <= 0) ctx->blocks_per_sm = 8;
   const char *env = getenv("PLSQR_BLOCKS_PER_SM");
   if (env && atoi(env) > 0) ctx->blocks_per_sm = atoi(env);
+  ctx->m2_blocks_per_sm = 48;
+  ctx->unroll = 2;
+  env = getenv("PLSQR_UNROLL");
+  if (env && (atoi(env) == 1 || atoi(env) == 2 || atoi(env) == 4)) ctx->unroll = atoi(env);
   return PLSQR_OK;
 }
 
@@ -309,11 +419,10 @@ int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
   if ((rc = ctx_init_common(ctx)) || (rc = upload_lines(ctx, k_csc, kp, &ctx->KC, n)) ||
       (rc = upload_lines(ctx, d_csr, dp, &ctx->D, m_d)) ||
       (rc = upload_lines(ctx, d_csc, dcp, &ctx->DC, n)) || (rc = build_kernel_rows(ctx)) ||
-      (rc = ctx_alloc_vectors(ctx))) {
+      (rc = ctx_alloc_vectors(ctx)) || (rc = plan_launch(ctx, kp))) {
     plsqr_ctx_destroy(ctx);
     return rc;
   }
-  plan_launch(ctx);
   if (o.precision == PLSQR_PREC_MIXED && (rc = mixed_prepare(ctx))) {
     plsqr_ctx_destroy(ctx);
     return rc;
@@ -410,15 +519,10 @@ int plsqr_get_b(plsqr_ctx *ctx, double *b_k) {
 
 // Enqueue one product on the context's stream.
 static int launch_aprod(plsqr_ctx *ctx, int mode, int scale_mode, bool with_parts) {
-  if (mode == 1) {
-    k_aprod1<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, ctx->stream>>>(
-        ctx->K.csr(), ctx->D.csr(), ctx->v, ctx->u, ctx->g1k, scale_mode, ctx->st,
-        with_parts ? ctx->parts_u : nullptr);
-  } else {
-    k_aprod2<kThreads><<<ctx->g2, kThreads, 0, ctx->stream>>>(
-        ctx->KC.csr(), ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, scale_mode, ctx->st,
-        with_parts ? ctx->parts_v : nullptr);
-  }
+  if (mode == 1)
+    m1(ctx, ctx->stream, scale_mode, with_parts ? ctx->parts_u : nullptr);
+  else
+    m2(ctx, ctx->stream, scale_mode, with_parts ? ctx->parts_v : nullptr);
   CK(cudaGetLastError());
   return PLSQR_OK;
 }
@@ -466,12 +570,10 @@ static int enqueue_iteration(plsqr_ctx *ctx, cudaStream_t s) {
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   double *se = ctx->want_se ? ctx->se : nullptr;
   const double *xref = ctx->has_ref ? ctx->xref : nullptr;
-  k_aprod1<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
-      ctx->K.csr(), ctx->D.csr(), ctx->v, ctx->u, ctx->g1k, kScaleNegAlpha, ctx->st, ctx->parts_u);
+  m1(ctx, s, kScaleNegAlpha, ctx->parts_u);
   k_norm_u<kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d,
                                                      ctx->st, 0);
-  k_aprod2<kThreads><<<ctx->g2, kThreads, 0, s>>>(ctx->KC.csr(), ctx->DC.csr(), ctx->u, ctx->m_k,
-                                                   ctx->v, kScaleNegBeta, ctx->st, ctx->parts_v);
+  m2(ctx, s, kScaleNegBeta, ctx->parts_v);
   k_update_x<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
       ctx->v, ctx->w, ctx->x, se, xref, ctx->n, ctx->parts_v, ctx->g2, ctx->st, ctx->parts_dk,
       xref ? ctx->parts_err : nullptr, ctx->hist, 0);
@@ -618,6 +720,53 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
                                cur.done ? -1 : r.itn, &r)))
       return rc;
   }
+  return PLSQR_OK;
+}
+
+int plsqr_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch) {
+  if (!ctx || (mode != 1 && mode != 2) || reps < 1 || !ms_per_launch) return PLSQR_ERR_ARG;
+  if (ctx->opts.precision == PLSQR_PREC_MIXED) return mixed_bench_aprod(ctx, mode, reps, ms_per_launch);
+  CK(cudaSetDevice(ctx->opts.device));
+  int rc;
+  if ((rc = launch_aprod(ctx, mode, kScaleOne, false))) return rc;  // warm-up
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int i = 0; i < reps; ++i)
+    if ((rc = launch_aprod(ctx, mode, kScaleOne, false))) return rc;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *ms_per_launch = (double)ms / reps;
+  return PLSQR_OK;
+}
+
+int plsqr_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration) {
+  if (!ctx || reps < 1 || !ms_per_iteration) return PLSQR_ERR_ARG;
+  if (ctx->opts.precision == PLSQR_PREC_MIXED) return mixed_bench_iteration(ctx, reps, ms_per_iteration);
+  if (!ctx->solved) return PLSQR_ERR_STATE;
+  CK(cudaSetDevice(ctx->opts.device));
+  int rc;
+  if (ctx->hist_cap < reps + 1) {  // every replay writes one history record
+    dev_free(ctx, ctx->hist);
+    ctx->hist = nullptr;
+    ctx->hist_cap = 0;
+    if ((rc = dev_alloc(ctx, &ctx->hist, (size_t)reps + 1))) return rc;
+    ctx->hist_cap = reps + 1;
+  }
+  if ((rc = ensure_graph(ctx))) return rc;
+  // continue from the state of the last solve, history from index 1
+  DevState h;
+  CK(cudaMemcpy(&h, ctx->st, sizeof(h), cudaMemcpyDeviceToHost));
+  h.itn = 0;
+  h.hist_base = 0;
+  CK(cudaMemcpy(ctx->st, &h, sizeof(h), cudaMemcpyHostToDevice));
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int i = 0; i < reps; ++i) CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *ms_per_iteration = (double)ms / reps;
   return PLSQR_OK;
 }
 

@@ -27,7 +27,10 @@ struct plsqr_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int32_t m_k = 0, m_d = 0, n = 0;
   int64_t nnz_k = 0, nnz_d = 0;
-  int sm_count = 0, blocks_per_sm = 0;
+  int sm_count = 0, blocks_per_sm = 0, unroll = 2;
+  int m2_blocks_per_sm = 48;
+  int32_t *kpart = nullptr, *cpart = nullptr;  // balanced warp -> line ranges
+  int32_t *corder = nullptr;                     // column visit order of A^T y
   DevLines K, D, KC, DC;  // kernel/damping by row, kernel/damping by column
   double *u = nullptr, *v = nullptr, *w = nullptr, *x = nullptr, *se = nullptr, *xref = nullptr;
   double *parts_u = nullptr, *parts_v = nullptr, *parts_dk = nullptr, *parts_err = nullptr;
@@ -69,3 +72,5 @@ int mixed_prepare(plsqr_ctx *ctx);
 int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, double *x,
                double *w, double *se, plsqr_iter *hist, plsqr_result *res);
 void mixed_free(plsqr_ctx *ctx);
+int mixed_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch);
+int mixed_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration);

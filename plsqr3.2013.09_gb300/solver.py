@@ -31,7 +31,7 @@ def _f64(a, n, name):
 class Context:
     def __init__(self, problem: Problem | None = None, *, files: dict | None = None,
                  precision: str = "fp64", device: int = 0, use_graph: bool = True,
-                 verbose: bool = False):
+                 verbose: bool = False, grid=None):
         L = N.lib()
         o = N.Opts()
         L.plsqr_default_opts(C.byref(o))
@@ -39,6 +39,10 @@ class Context:
         o.precision = N.PREC_MIXED if precision == "mixed" else N.PREC_FP64
         o.use_graph = int(use_graph)
         o.verbose = int(verbose)
+        if grid is None and problem is not None:
+            grid = problem.meta.get("grid")
+        if grid is not None:
+            o.grid[0], o.grid[1], o.grid[2] = (int(g) for g in grid)
         h = N.vp()
         if files is not None:
             f = N.Files()
@@ -57,6 +61,9 @@ class Context:
             N.check(L.plsqr_ctx_create(C.byref(k), C.byref(d), C.byref(dc), C.byref(o),
                                        C.byref(h)), "plsqr_ctx_create")
         self._h = h
+        # the right-hand side lsqr() uses when none is given: the problem's
+        # b_k, or (files) the one the library loaded
+        self._b = None if problem is None else np.ascontiguousarray(problem.b_k, np.float64)
         self.precision = precision
         info = self.info()
         self.m_k, self.m_d, self.n = info["m_k"], info["m_d"], info["n"]
@@ -141,7 +148,7 @@ class Context:
         a.want_se, a.stop_on_istop = int(want_se), int(stop_on_istop)
         a.result_txt = result_txt.encode() if result_txt else None
         a.sweeps, a.inner = sweeps, inner
-        b = None if b_k is None else _f64(b_k, self.m_k, "b_k")
+        b = self._b if b_k is None else _f64(b_k, self.m_k, "b_k")
         n_hist = (sweeps * inner if self.precision == "mixed" else lsqr_iteration) + 1
         x = np.empty(self.n)
         w = np.empty(self.n) if want_w else None
@@ -152,6 +159,21 @@ class Context:
                                        N.ptr(se), N.ptr(hist), C.byref(r)), "plsqr_lsqr")
         res = {k: getattr(r, k) for k, _ in N.Result._fields_ if k != "pad"}
         return dict(x=x, w=w, se=se, hist=hist, result=res)
+
+    # -- measurement ----------------------------------------------------------
+    def bench_aprod(self, mode: int, reps: int = 10) -> float:
+        """ms per launch of the mode-1/2 product kernel (overwrites u, v)."""
+        ms = N.f64(0)
+        self._check(N.lib().plsqr_bench_aprod(self._h, mode, reps, C.byref(ms)),
+                    "plsqr_bench_aprod")
+        return float(ms.value)
+
+    def bench_iteration(self, reps: int = 10) -> float:
+        """ms per LSQR iteration replayed from its CUDA graph."""
+        ms = N.f64(0)
+        self._check(N.lib().plsqr_bench_iteration(self._h, reps, C.byref(ms)),
+                    "plsqr_bench_iteration")
+        return float(ms.value)
 
     def get_x(self):
         x = np.empty(self.n)

@@ -31,6 +31,9 @@ CONFIGS: dict[str, dict] = {
                    blob_sigma=3.0, checker_amp=0.1, checker_period=8, noise_frac=0.01,
                    value_scale=1e-2, damp_identity=0.5, damp_lap=1.0, seed=0, iterations=300),
 }
+# the 96x96x32 grid with a tenth of the rays (~1.3e8 kernel nonzeros, ~3 GB on
+# the device): large enough to stream from HBM, small enough to profile
+CONFIGS["grid96s"] = dict(CONFIGS["grid96"], n_rays=20000)
 
 # the reference's file names for a generated problem (data/LSQR_run/LSQR3.pbs:10)
 FILE_NAMES = dict(ker_f="matrix_bycol.mm2.bin", ker_i="matrix_bycol.mm2.info",
