@@ -26,12 +26,15 @@ struct DevState {
   int32_t pad0;
 };
 
-// One compressed-sparse operand as the kernels see it.
-struct Csr {
+// One compressed-sparse operand as the kernels see it, with values of type T
+// (FP64, or the FP32 high half of the value split).
+template <typename T>
+struct CsrT {
   const int64_t *ptr;
   const int32_t *idx;
-  const double *val;
+  const T *val;
   int32_t n_lines;
 };
+using Csr = CsrT<double>;
 
 }  // namespace plsqr

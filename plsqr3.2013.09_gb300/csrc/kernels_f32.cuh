@@ -12,6 +12,7 @@
 
 namespace plsqr {
 
+// The kernel matrix by row with both halves of the value split.
 struct CsrF {
   const int64_t *ptr;
   const int32_t *idx;
@@ -19,47 +20,6 @@ struct CsrF {
   const float *lo;
   int32_t n_lines;
 };
-
-// Sum of hi[e] * x[idx[e]] over [beg, end) by one warp, FP32, 16-byte loads.
-__device__ __forceinline__ float warp_dot_f32(const int32_t *__restrict__ idx,
-                                              const float *__restrict__ val,
-                                              const float *__restrict__ x, int64_t beg,
-                                              int64_t end, int lane) {
-  float acc0 = 0.f, acc1 = 0.f;
-  int64_t a4 = (beg + 3) & ~int64_t(3);
-  if (a4 > end) a4 = end;
-  if (beg + lane < a4) acc0 = val[beg + lane] * x[idx[beg + lane]];
-  const int64_t e4 = a4 + ((end - a4) & ~int64_t(3));
-  const int4 *__restrict__ idx4 = reinterpret_cast<const int4 *>(idx);
-  const float4 *__restrict__ val4 = reinterpret_cast<const float4 *>(val);
-  int64_t g = (a4 >> 2) + lane;
-  const int64_t gend = e4 >> 2;
-  for (; g + 32 < gend; g += 64) {
-    const int4 c0 = __ldg(idx4 + g), c1 = __ldg(idx4 + g + 32);
-    const float4 v0 = __ldg(val4 + g), v1 = __ldg(val4 + g + 32);
-    acc0 = fmaf(v0.x, __ldg(x + c0.x), acc0);
-    acc1 = fmaf(v0.y, __ldg(x + c0.y), acc1);
-    acc0 = fmaf(v0.z, __ldg(x + c0.z), acc0);
-    acc1 = fmaf(v0.w, __ldg(x + c0.w), acc1);
-    acc0 = fmaf(v1.x, __ldg(x + c1.x), acc0);
-    acc1 = fmaf(v1.y, __ldg(x + c1.y), acc1);
-    acc0 = fmaf(v1.z, __ldg(x + c1.z), acc0);
-    acc1 = fmaf(v1.w, __ldg(x + c1.w), acc1);
-  }
-  if (g < gend) {
-    const int4 c0 = __ldg(idx4 + g);
-    const float4 v0 = __ldg(val4 + g);
-    acc0 = fmaf(v0.x, __ldg(x + c0.x), acc0);
-    acc1 = fmaf(v0.y, __ldg(x + c0.y), acc1);
-    acc0 = fmaf(v0.z, __ldg(x + c0.z), acc0);
-    acc1 = fmaf(v0.w, __ldg(x + c0.w), acc1);
-  }
-  if (e4 + lane < end) acc1 = fmaf(val[e4 + lane], x[idx[e4 + lane]], acc1);
-  float s = acc0 + acc1;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  return s;
-}
 
 // Sum of (hi[e] + lo[e]) * x[idx[e]] in FP64 by one warp.
 __device__ __forceinline__ double warp_dot_hilo(const int32_t *__restrict__ idx,
@@ -108,15 +68,16 @@ static __global__ void k_split_hilo(const double *__restrict__ v, int64_t nnz, f
 // values FP64), into u; per-block partial sums of squares as k_aprod1.
 template <int kThreads>
 __global__ void __launch_bounds__(kThreads)
-    k_residual(CsrF K, Csr D, const double *__restrict__ x, const double *__restrict__ b,
-               double *__restrict__ u, int gk, double *__restrict__ parts) {
+    k_residual(CsrF K, Csr D, const int32_t *__restrict__ kpart, const double *__restrict__ x,
+               const double *__restrict__ b, double *__restrict__ u, int gk,
+               double *__restrict__ parts) {
   __shared__ double smem[kThreads / 32];
   double sq = 0.0;
   if ((int)blockIdx.x < gk) {
     const int lane = threadIdx.x & 31;
-    const int warps_total = gk * (kThreads / 32);
-    for (int r = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); r < K.n_lines;
-         r += warps_total) {
+    const int w = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+    const int r1 = kpart[w + 1];
+    for (int r = kpart[w]; r < r1; ++r) {
       const double t = warp_dot_hilo(K.idx, K.hi, K.lo, x, K.ptr[r], K.ptr[r + 1], lane);
       if (lane == 0) {
         const double y = b[r] - t;
@@ -144,98 +105,6 @@ static __global__ void k_to_f32(const double *__restrict__ u, int64_t m, float *
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
        i += (int64_t)gridDim.x * blockDim.x)
     uf[i] = __double2float_rn(u[i]);
-}
-
-// Inner mode 1: u = -alpha u + A v (FP32), partial ||u||^2 in FP64.
-template <int kThreads>
-__global__ void __launch_bounds__(kThreads)
-    k_aprod1_f32(CsrF K, Csr D, const float *__restrict__ v, float *__restrict__ u, int gk,
-                 const DevState *__restrict__ st, double *__restrict__ parts) {
-  __shared__ double smem[kThreads / 32];
-  const float s = (float)(-st->alpha);
-  double sq = 0.0;
-  if ((int)blockIdx.x < gk) {
-    const int lane = threadIdx.x & 31;
-    const int warps_total = gk * (kThreads / 32);
-    for (int r = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); r < K.n_lines;
-         r += warps_total) {
-      const float t = warp_dot_f32(K.idx, K.hi, v, K.ptr[r], K.ptr[r + 1], lane);
-      if (lane == 0) {
-        const float y = fmaf(s, u[r], t);
-        u[r] = y;
-        sq = fma((double)y, (double)y, sq);
-      }
-    }
-  } else {
-    const int gd = gridDim.x - gk;
-    float *ud = u + K.n_lines;
-    for (int r = (blockIdx.x - gk) * kThreads + threadIdx.x; r < D.n_lines; r += gd * kThreads) {
-      float t = 0.f;
-      for (int64_t e = D.ptr[r]; e < D.ptr[r + 1]; ++e) t = fmaf((float)D.val[e], v[D.idx[e]], t);
-      const float y = fmaf(s, ud[r], t);
-      ud[r] = y;
-      sq = fma((double)y, (double)y, sq);
-    }
-  }
-  const double bs = block_sum<kThreads>(sq, smem);
-  if (threadIdx.x == 0) parts[blockIdx.x] = bs;
-}
-
-// Inner N1: beta, u *= 1/beta (FP32 vector, FP64 scalars).
-template <int kThreads>
-__global__ void __launch_bounds__(kThreads)
-    k_norm_u_f32(float *__restrict__ u, int64_t m, const double *__restrict__ parts, int gk,
-                 int gd, DevState *__restrict__ st) {
-  __shared__ double smem[kThreads / 32];
-  __shared__ double s_rb;
-  const double sk = sum_parts<kThreads>(parts, gk, smem);
-  const double sd = sum_parts<kThreads>(parts + gk, gd, smem);
-  if (threadIdx.x == 0) {
-    const double beta = __dsqrt_rn(dadd(sk, sd));
-    s_rb = beta > 0.0 ? ddiv(1.0, beta) : 0.0;
-    if (blockIdx.x == 0) {
-      st->beta = beta;
-      st->s_beta_pos = beta > 0.0;
-      double temp = d2norm(st->alpha, beta);
-      temp = d2norm(temp, st->damp);
-      st->anorm = d2norm(st->anorm, temp);
-    }
-  }
-  __syncthreads();
-  if (s_rb == 0.0) return;
-  const float rb = (float)s_rb;
-  for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < m;
-       i += (int64_t)gridDim.x * kThreads)
-    u[i] *= rb;
-}
-
-// Inner mode 2: v = s v + (K^T u_k + D^T u_d) (FP32), partial ||v||^2 in FP64.
-// start = 1: v = A^T u (s = 0).  Skipped when beta == 0.
-template <int kThreads>
-__global__ void __launch_bounds__(kThreads)
-    k_aprod2_f32(CsrF KC, Csr DC, const float *__restrict__ u, int m_k, float *__restrict__ v,
-                 int start, const DevState *__restrict__ st, double *__restrict__ parts) {
-  __shared__ double smem[kThreads / 32];
-  if (!st->s_beta_pos) return;
-  const float s = start ? 0.f : (float)(-st->beta);
-  const float *ud = u + m_k;
-  const int lane = threadIdx.x & 31;
-  const int warps_total = gridDim.x * (kThreads / 32);
-  double sq = 0.0;
-  for (int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); c < KC.n_lines;
-       c += warps_total) {
-    const float sk = warp_dot_f32(KC.idx, KC.hi, u, KC.ptr[c], KC.ptr[c + 1], lane);
-    if (lane == 0) {
-      float sd = 0.f;
-      for (int64_t e = DC.ptr[c]; e < DC.ptr[c + 1]; ++e)
-        sd = fmaf((float)DC.val[e], ud[DC.idx[e]], sd);
-      const float y = start ? (sk + sd) : fmaf(s, v[c], sk + sd);
-      v[c] = y;
-      sq = fma((double)y, (double)y, sq);
-    }
-  }
-  const double bs = block_sum<kThreads>(sq, smem);
-  if (threadIdx.x == 0) parts[blockIdx.x] = bs;
 }
 
 // Inner N2: alpha, v *= 1/alpha, FP64 rotation, FP32 dx/w update; error of

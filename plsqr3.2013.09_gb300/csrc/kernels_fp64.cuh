@@ -23,55 +23,83 @@
 
 namespace plsqr {
 
+__device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Four consecutive values, 16-byte aligned, in 16-byte loads.
+__device__ __forceinline__ void load4(const double *v, int64_t g, double (&o)[4]) {
+  const double2 a = __ldg(reinterpret_cast<const double2 *>(v) + 2 * g);
+  const double2 b = __ldg(reinterpret_cast<const double2 *>(v) + 2 * g + 1);
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = b.x;
+  o[3] = b.y;
+}
+__device__ __forceinline__ void load4(const float *v, int64_t g, float (&o)[4]) {
+  const float4 a = __ldg(reinterpret_cast<const float4 *>(v) + g);
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = a.z;
+  o[3] = a.w;
+}
+
 // This lane's share of sum val[e] * x[idx[e]] over [beg, end) when one warp
-// streams the range: 16-byte loads of 4 indices and 2x2 values per lane and
-// step, kUnroll steps in flight.  Reduce across the warp with warp_sum.
-template <int kUnroll>
-__device__ __forceinline__ double lane_dot_f64(const int32_t *__restrict__ idx,
-                                               const double *__restrict__ val,
-                                               const double *__restrict__ x, int64_t beg,
-                                               int64_t end, int lane) {
-  double acc0 = 0.0, acc1 = 0.0;
+// streams the range: per lane and step one 16-byte load of 4 indices and the
+// 4 values (16 or 32 bytes), kUnroll steps in flight.  Reduce across the warp
+// with warp_sum.
+template <typename T, int kUnroll>
+__device__ __forceinline__ T lane_dot(const int32_t *__restrict__ idx, const T *__restrict__ val,
+                                      const T *__restrict__ x, int64_t beg, int64_t end,
+                                      int lane) {
+  T acc0 = 0, acc1 = 0;
   // head: up to 3 elements until beg is a multiple of 4
   int64_t a4 = (beg + 3) & ~int64_t(3);
   if (a4 > end) a4 = end;
   if (beg + lane < a4) acc0 = val[beg + lane] * x[idx[beg + lane]];
   const int64_t e4 = a4 + ((end - a4) & ~int64_t(3));
   const int4 *__restrict__ idx4 = reinterpret_cast<const int4 *>(idx);
-  const double2 *__restrict__ val2 = reinterpret_cast<const double2 *>(val);
   int64_t g = (a4 >> 2) + lane;
   const int64_t gend = e4 >> 2;
   for (; g + 32 * (kUnroll - 1) < gend; g += 32 * kUnroll) {
     int4 c[kUnroll];
-    double2 v0[kUnroll], v1[kUnroll];
+    T v[kUnroll][4];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      c[u] = __ldg(idx4 + g + 32 * u);
-      v0[u] = __ldg(val2 + 2 * (g + 32 * u));
-      v1[u] = __ldg(val2 + 2 * (g + 32 * u) + 1);
+    for (int q = 0; q < kUnroll; ++q) {
+      c[q] = __ldg(idx4 + g + 32 * q);
+      load4(val, g + 32 * q, v[q]);
     }
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      acc0 = fma(v0[u].x, __ldg(x + c[u].x), acc0);
-      acc1 = fma(v0[u].y, __ldg(x + c[u].y), acc1);
-      acc0 = fma(v1[u].x, __ldg(x + c[u].z), acc0);
-      acc1 = fma(v1[u].y, __ldg(x + c[u].w), acc1);
+    for (int q = 0; q < kUnroll; ++q) {
+      acc0 = fmaT(v[q][0], __ldg(x + c[q].x), acc0);
+      acc1 = fmaT(v[q][1], __ldg(x + c[q].y), acc1);
+      acc0 = fmaT(v[q][2], __ldg(x + c[q].z), acc0);
+      acc1 = fmaT(v[q][3], __ldg(x + c[q].w), acc1);
     }
   }
   for (; g < gend; g += 32) {
     const int4 c0 = __ldg(idx4 + g);
-    const double2 v0 = __ldg(val2 + 2 * g), v1 = __ldg(val2 + 2 * g + 1);
-    acc0 = fma(v0.x, __ldg(x + c0.x), acc0);
-    acc1 = fma(v0.y, __ldg(x + c0.y), acc1);
-    acc0 = fma(v1.x, __ldg(x + c0.z), acc0);
-    acc1 = fma(v1.y, __ldg(x + c0.w), acc1);
+    T v0[4];
+    load4(val, g, v0);
+    acc0 = fmaT(v0[0], __ldg(x + c0.x), acc0);
+    acc1 = fmaT(v0[1], __ldg(x + c0.y), acc1);
+    acc0 = fmaT(v0[2], __ldg(x + c0.z), acc0);
+    acc1 = fmaT(v0[3], __ldg(x + c0.w), acc1);
   }
   // tail: up to 3 elements
-  if (e4 + lane < end) acc1 = fma(val[e4 + lane], x[idx[e4 + lane]], acc1);
+  if (e4 + lane < end) acc1 = fmaT(val[e4 + lane], x[idx[e4 + lane]], acc1);
   return acc0 + acc1;
 }
 
-__device__ __forceinline__ double warp_sum(double s) {
+template <int kUnroll>
+__device__ __forceinline__ double lane_dot_f64(const int32_t *__restrict__ idx,
+                                               const double *__restrict__ val,
+                                               const double *__restrict__ x, int64_t beg,
+                                               int64_t end, int lane) {
+  return lane_dot<double, kUnroll>(idx, val, x, beg, end, lane);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T s) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   return s;
@@ -129,16 +157,37 @@ enum ScaleMode : int {
   kScaleZero = 3,      // LSQR start-up: v = 0 + A^T u
 };
 
+// Updated vector element y = s*old + t, rounded like the reference's dscal
+// followed by the += of the product (FP64), or one FP32 fma.
+__device__ __forceinline__ double scaled_add(double s, double old, double t) {
+  return dadd(dmul(s, old), t);
+}
+__device__ __forceinline__ float scaled_add(double s, float old, float t) {
+  return fmaf((float)s, old, t);
+}
+
+// Damping row r times x, in stored order; FP64: mul and add rounded apart as
+// in CPUSpMV.c:67-70, FP32: the FP64 values rounded to FP32.
+__device__ __forceinline__ double damp_row(const Csr &D, const double *__restrict__ x, int r) {
+  return seq_dot_f64(D.idx, D.val, x, D.ptr[r], D.ptr[r + 1]);
+}
+__device__ __forceinline__ float damp_row(const Csr &D, const float *__restrict__ x, int r) {
+  float t = 0.f;
+  for (int64_t e = D.ptr[r]; e < D.ptr[r + 1]; ++e) t = fmaf((float)D.val[e], x[D.idx[e]], t);
+  return t;
+}
+
 // ---------------------------------------------------------------------------
 // M1: u_k[r] = s*u_k[r] + (K v)[r], u_d[r] = s*u_d[r] + (D v)[r]; per-block
-// partial sums of squares of the new u: parts[0..gk) kernel rows,
+// partial sums of squares of the new u (in FP64): parts[0..gk) kernel rows,
 // parts[gk..gk+gd) damping rows.  Warp w of the kernel blocks owns rows
 // [kpart[w], kpart[w+1]), a contiguous range holding about the same number of
-// nonzeros as every other warp's.
-template <int kThreads, int kUnroll>
+// nonzeros as every other warp's.  T = double: the FP64 solver; T = float:
+// the inner sweeps of the mixed solver (values: the FP32 high half).
+template <typename T, int kThreads, int kUnroll>
 __global__ void __launch_bounds__(kThreads)
-    k_aprod1(Csr K, Csr D, const int32_t *__restrict__ kpart, const double *__restrict__ v,
-             double *__restrict__ u, int gk, int mode, const DevState *__restrict__ st,
+    k_aprod1(CsrT<T> K, Csr D, const int32_t *__restrict__ kpart, const T *__restrict__ v,
+             T *__restrict__ u, int gk, int mode, const DevState *__restrict__ st,
              double *__restrict__ parts) {
   __shared__ double smem[kThreads / 32];
   double s = 1.0;
@@ -149,23 +198,21 @@ __global__ void __launch_bounds__(kThreads)
     const int w = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
     const int r1 = kpart[w + 1];
     for (int r = kpart[w]; r < r1; ++r) {
-      const double t =
-          warp_sum(lane_dot_f64<kUnroll>(K.idx, K.val, v, K.ptr[r], K.ptr[r + 1], lane));
+      const T t = warp_sum(lane_dot<T, kUnroll>(K.idx, K.val, v, K.ptr[r], K.ptr[r + 1], lane));
       if (lane == 0) {
-        const double y = dadd(dmul(s, u[r]), t);  // dscal, then y_k += t_k
+        const T y = scaled_add(s, u[r], t);  // dscal, then y_k += t_k
         u[r] = y;
-        sq = fma(y, y, sq);
+        sq = fma((double)y, (double)y, sq);
       }
     }
   } else {
     const int gd = gridDim.x - gk;
-    double *ud = u + K.n_lines;
+    T *ud = u + K.n_lines;
     for (int r = (blockIdx.x - gk) * kThreads + threadIdx.x; r < D.n_lines;
          r += gd * kThreads) {
-      const double t = seq_dot_f64(D.idx, D.val, v, D.ptr[r], D.ptr[r + 1]);
-      const double y = dadd(dmul(s, ud[r]), t);
+      const T y = scaled_add(s, ud[r], damp_row(D, v, r));
       ud[r] = y;
-      sq = fma(y, y, sq);
+      sq = fma((double)y, (double)y, sq);
     }
   }
   const double b = block_sum<kThreads>(sq, smem);
@@ -175,10 +222,13 @@ __global__ void __launch_bounds__(kThreads)
 // ---------------------------------------------------------------------------
 // N1: beta = sqrt(sum_k + sum_d); u *= 1/beta.  LSQR start-up (start = 1)
 // also takes this path with beta = ||b||.
-template <int kThreads>
+__device__ __forceinline__ double scale_elem(double x, double r) { return dmul(x, r); }
+__device__ __forceinline__ float scale_elem(float x, double r) { return x * (float)r; }
+
+template <typename T, int kThreads>
 __global__ void __launch_bounds__(kThreads)
-    k_norm_u(double *__restrict__ u, int64_t m, const double *__restrict__ parts, int gk,
-             int gd, DevState *__restrict__ st, int start) {
+    k_norm_u(T *__restrict__ u, int64_t m, const double *__restrict__ parts, int gk, int gd,
+             DevState *__restrict__ st, int start) {
   __shared__ double smem[kThreads / 32];
   __shared__ double s_rb;
   const double sk = sum_parts<kThreads>(parts, gk, smem);
@@ -201,7 +251,7 @@ __global__ void __launch_bounds__(kThreads)
   if (rb == 0.0) return;  // beta == 0: u is left as is
   for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < m;
        i += (int64_t)gridDim.x * kThreads)
-    u[i] = dmul(u[i], rb);
+    u[i] = scale_elem(u[i], rb);
 }
 
 // ---------------------------------------------------------------------------
@@ -214,11 +264,12 @@ __global__ void __launch_bounds__(kThreads)
 // are streamed by the whole warp and its damping entries (a few per column)
 // are spread over the lanes, so every FP64 instruction runs on a full warp.
 // In LSQR mode the kernel is skipped when beta == 0 (source/lsqr.c:530).
-template <int kThreads, int kUnroll>
+template <typename T, int kThreads, int kUnroll>
 __global__ void __launch_bounds__(kThreads)
-    k_aprod2(Csr KC, Csr DC, const int32_t *__restrict__ cpart, const int32_t *__restrict__ corder,
-             const double *__restrict__ u, int m_k, double *__restrict__ v, int mode,
-             const DevState *__restrict__ st, double *__restrict__ parts) {
+    k_aprod2(CsrT<T> KC, Csr DC, const int32_t *__restrict__ cpart,
+             const int32_t *__restrict__ corder, const T *__restrict__ u, int m_k,
+             T *__restrict__ v, int mode, const DevState *__restrict__ st,
+             double *__restrict__ parts) {
   __shared__ double smem[kThreads / 32];
   double s = 1.0;
   if (mode == kScaleNegBeta) {
@@ -228,20 +279,20 @@ __global__ void __launch_bounds__(kThreads)
     if (!st->s_beta_pos) return;
     s = 0.0;
   }
-  const double *ud = u + m_k;
+  const T *ud = u + m_k;
   const int lane = threadIdx.x & 31;
   const int c1 = cpart[blockIdx.x + 1];
   double sq = 0.0;
   for (int k = cpart[blockIdx.x] + (threadIdx.x >> 5); k < c1; k += kThreads / 32) {
     const int c = corder[k];
-    double acc = lane_dot_f64<kUnroll>(KC.idx, KC.val, u, KC.ptr[c], KC.ptr[c + 1], lane);
+    T acc = lane_dot<T, kUnroll>(KC.idx, KC.val, u, KC.ptr[c], KC.ptr[c + 1], lane);
     for (int64_t e = DC.ptr[c] + lane; e < DC.ptr[c + 1]; e += 32)
-      acc = fma(DC.val[e], ud[DC.idx[e]], acc);
-    const double t = warp_sum(acc);
+      acc = fmaT((T)DC.val[e], ud[DC.idx[e]], acc);
+    const T t = warp_sum(acc);
     if (lane == 0) {
-      const double y = dadd(dmul(s, v[c]), t);  // x += (s_k + s_d)
+      const T y = scaled_add(s, v[c], t);  // x += (s_k + s_d)
       v[c] = y;
-      sq = fma(y, y, sq);
+      sq = fma((double)y, (double)y, sq);
     }
   }
   const double b = block_sum<kThreads>(sq, smem);

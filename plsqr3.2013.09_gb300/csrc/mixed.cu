@@ -19,6 +19,7 @@
 
 #include "kernels_f32.cuh"
 #include "plsqr_internal.h"
+#include "slab.cuh"
 
 using namespace plsqr;
 
@@ -28,6 +29,10 @@ constexpr int kThreads = 256;
 
 struct MixedState {
   float *k_hi = nullptr, *k_lo = nullptr, *kc_hi = nullptr;
+  // FP32 slab layouts (high half of the split, 6 bytes per nonzero) used by
+  // the inner sweeps when the FP64 context uses slabs
+  bool slabs = false;
+  DevSlab<float> s_rows, s_cols;
   float *uf = nullptr, *vf = nullptr, *wf = nullptr, *dxf = nullptr;
   double *b = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -71,28 +76,78 @@ int mixed_prepare(plsqr_ctx *ctx) {
   k_split_hilo<<<g, 256, 0, ctx->stream>>>(ctx->KC.val, ctx->nnz_k, M->kc_hi, nullptr);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->slab_ok) {
+    const int slab = 49152;  // 192 KB of FP32 per block
+    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, &M->s_rows)) ||
+        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, &M->s_cols)))
+      return rc;
+    CK(cudaFuncSetAttribute(k_slab_spmv<float, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)std::max(M->s_rows.smem, M->s_cols.smem)));
+    M->slabs = true;
+  }
   return PLSQR_OK;
 }
 
-static CsrF rows_f(const plsqr_ctx *ctx) {
+// partial-sum counts of the inner products (slab combine grids or per-line grids)
+static int pu_k(const plsqr_ctx *ctx) { return ctx->mixed->slabs ? ctx->gc1k : ctx->g1k; }
+static int pu_d(const plsqr_ctx *ctx) { return ctx->mixed->slabs ? ctx->gc1d : ctx->g1d; }
+static int pv(const plsqr_ctx *ctx) { return ctx->mixed->slabs ? ctx->gc2 : ctx->g2; }
+
+static CsrF rows_hilo(const plsqr_ctx *ctx) {
   return CsrF{ctx->K.ptr, ctx->K.idx, ctx->mixed->k_hi, ctx->mixed->k_lo, ctx->K.n_lines};
 }
-static CsrF cols_f(const plsqr_ctx *ctx) {
-  return CsrF{ctx->KC.ptr, ctx->KC.idx, ctx->mixed->kc_hi, nullptr, ctx->KC.n_lines};
+static CsrT<float> rows_f(const plsqr_ctx *ctx) {
+  return CsrT<float>{ctx->K.ptr, ctx->K.idx, ctx->mixed->k_hi, ctx->K.n_lines};
+}
+static CsrT<float> cols_f(const plsqr_ctx *ctx) {
+  return CsrT<float>{ctx->KC.ptr, ctx->KC.idx, ctx->mixed->kc_hi, ctx->KC.n_lines};
+}
+// the inner sweeps' products: the FP64 kernels instantiated for FP32, on the
+// FP32 slabs when present
+static SlabCsr<float> view(const DevSlab<float> &S) {
+  return SlabCsr<float>{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx};
+}
+static void m1f(plsqr_ctx *ctx, cudaStream_t s) {
+  MixedState *M = ctx->mixed;
+  if (M->slabs) {
+    const DevSlab<float> &S = M->s_rows;
+    k_slab_spmv<float, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(view(S), S.lpart, S.bps, M->vf,
+                                                                     S.partial);
+    k_combine_rows<float, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
+        S.partial, S.n_slabs, ctx->m_k, ctx->D.csr(), M->vf, M->uf, ctx->gc1k, kScaleNegAlpha,
+        ctx->st, ctx->parts_u);
+    return;
+  }
+  k_aprod1<float, kThreads, 2><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
+      rows_f(ctx), ctx->D.csr(), ctx->kpart, M->vf, M->uf, ctx->g1k, kScaleNegAlpha, ctx->st,
+      ctx->parts_u);
+}
+static void m2f(plsqr_ctx *ctx, cudaStream_t s, int mode) {
+  MixedState *M = ctx->mixed;
+  if (M->slabs) {
+    const DevSlab<float> &S = M->s_cols;
+    k_slab_spmv<float, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(view(S), S.lpart, S.bps, M->uf,
+                                                                     S.partial);
+    k_combine_cols<float, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+        S.partial, S.n_slabs, ctx->n, ctx->DC.csr(), M->uf, ctx->m_k, M->vf, mode, ctx->st,
+        ctx->parts_v);
+    return;
+  }
+  k_aprod2<float, kThreads, 2><<<ctx->g2, kThreads, 0, s>>>(
+      cols_f(ctx), ctx->DC.csr(), ctx->cpart, ctx->corder, M->uf, ctx->m_k, M->vf, mode, ctx->st,
+      ctx->parts_v);
 }
 
 static int enqueue_inner(plsqr_ctx *ctx, cudaStream_t s) {
   MixedState *M = ctx->mixed;
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   const double *xref = ctx->has_ref ? ctx->xref : nullptr;
-  k_aprod1_f32<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
-      rows_f(ctx), ctx->D.csr(), M->vf, M->uf, ctx->g1k, ctx->st, ctx->parts_u);
-  k_norm_u_f32<kThreads><<<ctx->gvu, kThreads, 0, s>>>(M->uf, m, ctx->parts_u, ctx->g1k, ctx->g1d,
-                                                       ctx->st);
-  k_aprod2_f32<kThreads><<<ctx->g2, kThreads, 0, s>>>(cols_f(ctx), ctx->DC.csr(), M->uf, ctx->m_k,
-                                                       M->vf, 0, ctx->st, ctx->parts_v);
+  m1f(ctx, s);
+  k_norm_u<float, kThreads><<<ctx->gvu, kThreads, 0, s>>>(M->uf, m, ctx->parts_u, pu_k(ctx),
+                                                          pu_d(ctx), ctx->st, 0);
+  m2f(ctx, s, kScaleNegBeta);
   k_update_dx_f32<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
-      M->vf, M->wf, M->dxf, ctx->x, xref, ctx->n, ctx->parts_v, ctx->g2, ctx->st, ctx->parts_dk,
+      M->vf, M->wf, M->dxf, ctx->x, xref, ctx->n, ctx->parts_v, pv(ctx), ctx->st, ctx->parts_dk,
       xref ? ctx->parts_err : nullptr, 0);
   k_tail<kThreads><<<1, kThreads, 0, s>>>(ctx->st, ctx->parts_dk, xref ? ctx->parts_err : nullptr,
                                            ctx->gvx, ctx->x, ctx->hist);
@@ -171,14 +226,13 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     if (ctx->has_ref) k_ref_norm<kThreads><<<1, kThreads, 0, ctx->stream>>>(ctx->xref, ctx->n, ctx->st);
     // outer residual and the start-up of the inner solve
     k_residual<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, ctx->stream>>>(
-        rows_f(ctx), ctx->D.csr(), ctx->x, M->b, ctx->u, ctx->g1k, ctx->parts_u);
-    k_norm_u<kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, ctx->parts_u, ctx->g1k,
-                                                                ctx->g1d, ctx->st, 1);
+        rows_hilo(ctx), ctx->D.csr(), ctx->kpart, ctx->x, M->b, ctx->u, ctx->g1k, ctx->parts_u);
+    k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(
+        ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d, ctx->st, 1);
     k_to_f32<<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, M->uf);
-    k_aprod2_f32<kThreads><<<ctx->g2, kThreads, 0, ctx->stream>>>(
-        cols_f(ctx), ctx->DC.csr(), M->uf, ctx->m_k, M->vf, 1, ctx->st, ctx->parts_v);
+    m2f(ctx, ctx->stream, kScaleZero);
     k_update_dx_f32<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
-        M->vf, M->wf, M->dxf, ctx->x, nullptr, ctx->n, ctx->parts_v, ctx->g2, ctx->st,
+        M->vf, M->wf, M->dxf, ctx->x, nullptr, ctx->n, ctx->parts_v, pv(ctx), ctx->st,
         ctx->parts_dk, nullptr, 1);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
@@ -233,15 +287,12 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
 int mixed_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch) {
   int rc;
   if ((rc = mixed_prepare(ctx))) return rc;
-  MixedState *M = ctx->mixed;
   CK(cudaSetDevice(ctx->opts.device));
   auto launch = [&]() {
     if (mode == 1)
-      k_aprod1_f32<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, ctx->stream>>>(
-          rows_f(ctx), ctx->D.csr(), M->vf, M->uf, ctx->g1k, ctx->st, ctx->parts_u);
+      m1f(ctx, ctx->stream);
     else
-      k_aprod2_f32<kThreads><<<ctx->g2, kThreads, 0, ctx->stream>>>(
-          cols_f(ctx), ctx->DC.csr(), M->uf, ctx->m_k, M->vf, 1, ctx->st, ctx->parts_v);
+      m2f(ctx, ctx->stream, kScaleZero);
   };
   // a state with beta > 0 and alpha = 0 so that both kernels run fully
   DevState h;

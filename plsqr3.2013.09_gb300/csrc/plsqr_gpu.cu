@@ -20,6 +20,7 @@
 
 #include "kernels_fp64.cuh"
 #include "plsqr_internal.h"
+#include "slab.cuh"
 #include "transpose.cuh"
 
 using namespace plsqr;
@@ -175,16 +176,29 @@ static void balanced_partition(const int64_t *ptr, int32_t n_lines, int parts,
 
 template <int U>
 static void launch_m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
-  k_aprod1<kThreads, U><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
+  k_aprod1<double, kThreads, U><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
       ctx->K.csr(), ctx->D.csr(), ctx->kpart, ctx->v, ctx->u, ctx->g1k, mode, ctx->st, parts);
 }
 template <int U>
 static void launch_m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
-  k_aprod2<kThreads, U><<<ctx->g2, kThreads, 0, s>>>(ctx->KC.csr(), ctx->DC.csr(), ctx->cpart,
+  k_aprod2<double, kThreads, U><<<ctx->g2, kThreads, 0, s>>>(ctx->KC.csr(), ctx->DC.csr(), ctx->cpart,
                                                       ctx->corder, ctx->u, ctx->m_k, ctx->v, mode,
                                                       ctx->st, parts);
 }
+// The products.  Slab path: slab SpMV into per-slab partials, then the
+// combine kernel (scale, damping part, sums of squares).  Otherwise the
+// per-line kernels.  Either way `parts` receives pu_k + pu_d (mode 1) or pv
+// (mode 2) per-block sums of squares for the norm kernels.
 static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  if (ctx->use_slabs) {
+    const DevSlab<double> &S = ctx->s_rows;
+    k_slab_spmv<double, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(
+        SlabCsr<double>{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx}, S.lpart, S.bps,
+        ctx->v, S.partial);
+    k_combine_rows<double, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
+        S.partial, S.n_slabs, ctx->m_k, ctx->D.csr(), ctx->v, ctx->u, ctx->gc1k, mode, ctx->st, parts);
+    return;
+  }
   switch (ctx->unroll) {
     case 1: launch_m1<1>(ctx, s, mode, parts); break;
     case 4: launch_m1<4>(ctx, s, mode, parts); break;
@@ -192,12 +206,35 @@ static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
   }
 }
 static void m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  if (ctx->use_slabs) {
+    const DevSlab<double> &S = ctx->s_cols;
+    k_slab_spmv<double, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(
+        SlabCsr<double>{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx}, S.lpart, S.bps,
+        ctx->u, S.partial);
+    k_combine_cols<double, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+        S.partial, S.n_slabs, ctx->n, ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, mode, ctx->st, parts);
+    return;
+  }
   switch (ctx->unroll) {
     case 1: launch_m2<1>(ctx, s, mode, parts); break;
     case 4: launch_m2<4>(ctx, s, mode, parts); break;
     default: launch_m2<2>(ctx, s, mode, parts);
   }
 }
+// The slab kernel stages up to 192 KB of shared memory; the limit is a
+// per-module attribute, so it is set here, where the kernel is launched.
+static int slab_attrs(plsqr_ctx *ctx) {
+  if (!ctx->use_slabs) return PLSQR_OK;
+  const size_t smem = std::max(ctx->s_rows.smem, ctx->s_cols.smem);
+  CK(cudaFuncSetAttribute(k_slab_spmv<double, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)smem));
+  return PLSQR_OK;
+}
+
+// partial-sum counts the norm kernels read
+int ctx_pu_k(const plsqr_ctx *ctx) { return ctx->use_slabs ? ctx->gc1k : ctx->g1k; }
+int ctx_pu_d(const plsqr_ctx *ctx) { return ctx->use_slabs ? ctx->gc1d : ctx->g1d; }
+int ctx_pv(const plsqr_ctx *ctx) { return ctx->use_slabs ? ctx->gc2 : ctx->g2; }
 
 // Spread the low 10 bits of v to every third bit.
 static uint32_t part1by2(uint32_t v) {
@@ -232,7 +269,7 @@ static int plan_launch(plsqr_ctx *ctx, const std::vector<int64_t> &kc_ptr) {
   const int sm = ctx->sm_count;
   const int wpb = kThreads / 32;
   int occ1 = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_aprod1<kThreads, 2>, kThreads, 0));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_aprod1<double, kThreads, 2>, kThreads, 0));
   occ1 = std::max(1, std::min(occ1, ctx->blocks_per_sm));
   // every reduction kernel writes one partial per block: at most kMaxParts
   const int half = kMaxParts / 2;
@@ -419,7 +456,8 @@ int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
   if ((rc = ctx_init_common(ctx)) || (rc = upload_lines(ctx, k_csc, kp, &ctx->KC, n)) ||
       (rc = upload_lines(ctx, d_csr, dp, &ctx->D, m_d)) ||
       (rc = upload_lines(ctx, d_csc, dcp, &ctx->DC, n)) || (rc = build_kernel_rows(ctx)) ||
-      (rc = ctx_alloc_vectors(ctx)) || (rc = plan_launch(ctx, kp))) {
+      (rc = ctx_alloc_vectors(ctx)) || (rc = plan_launch(ctx, kp)) || (rc = slab_plan(ctx)) ||
+      (rc = slab_attrs(ctx))) {
     plsqr_ctx_destroy(ctx);
     return rc;
   }
@@ -571,11 +609,11 @@ static int enqueue_iteration(plsqr_ctx *ctx, cudaStream_t s) {
   double *se = ctx->want_se ? ctx->se : nullptr;
   const double *xref = ctx->has_ref ? ctx->xref : nullptr;
   m1(ctx, s, kScaleNegAlpha, ctx->parts_u);
-  k_norm_u<kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d,
-                                                     ctx->st, 0);
+  k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->parts_u, ctx_pu_k(ctx),
+                                                             ctx_pu_d(ctx), ctx->st, 0);
   m2(ctx, s, kScaleNegBeta, ctx->parts_v);
   k_update_x<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
-      ctx->v, ctx->w, ctx->x, se, xref, ctx->n, ctx->parts_v, ctx->g2, ctx->st, ctx->parts_dk,
+      ctx->v, ctx->w, ctx->x, se, xref, ctx->n, ctx->parts_v, ctx_pv(ctx), ctx->st, ctx->parts_dk,
       xref ? ctx->parts_err : nullptr, ctx->hist, 0);
   k_tail<kThreads><<<1, kThreads, 0, s>>>(ctx->st, ctx->parts_dk, xref ? ctx->parts_err : nullptr,
                                            ctx->gvx, ctx->x, ctx->hist);
@@ -647,12 +685,12 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   k_sumsq_u<kThreads><<<ctx->gsk + ctx->gsd, kThreads, 0, ctx->stream>>>(ctx->u, ctx->m_k, ctx->m_d,
                                                                           ctx->gsk, ctx->parts_u);
-  k_norm_u<kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, ctx->parts_u, ctx->gsk,
+  k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, ctx->parts_u, ctx->gsk,
                                                               ctx->gsd, ctx->st, 1);
   if ((rc = launch_aprod(ctx, 2, kScaleZero, true))) return rc;
   k_update_x<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
       ctx->v, ctx->w, ctx->x, ctx->want_se ? ctx->se : nullptr, nullptr, ctx->n, ctx->parts_v,
-      ctx->g2, ctx->st, ctx->parts_dk, nullptr, ctx->hist, 1);
+      ctx_pv(ctx), ctx->st, ctx->parts_dk, nullptr, ctx->hist, 1);
   CK(cudaGetLastError());
   DevState cur;
   CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));

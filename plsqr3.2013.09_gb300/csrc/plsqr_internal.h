@@ -19,6 +19,20 @@ struct DevLines {
   plsqr::Csr csr() const { return plsqr::Csr{ptr, idx, val, n_lines}; }
 };
 
+// One operand in the slab layout (slab.cuh), with its block partition.
+template <typename T>
+struct DevSlab {
+  int64_t *ptr = nullptr;
+  uint16_t *idx = nullptr;
+  T *val = nullptr;
+  int32_t n_lines = 0, n_slabs = 0, slab = 0, n_idx = 0;
+  int64_t nnz_padded = 0;
+  int32_t *lpart = nullptr;  // [n_slabs * (bps + 1)] line ranges of the blocks
+  int bps = 0;               // blocks per slab
+  T *partial = nullptr;      // [n_slabs * n_lines]
+  size_t smem = 0;           // shared memory per block
+};
+
 struct MixedState;  // mixed.cu
 
 struct plsqr_ctx {
@@ -47,7 +61,21 @@ struct plsqr_ctx {
   int64_t device_bytes = 0;
   char last_error[512] = {0};
   MixedState *mixed = nullptr;
+  // slab layout of the kernel matrix (default FP64 product path)
+  bool use_slabs = false;  // FP64 products on slabs (opt-in)
+  bool slab_ok = false;    // dimensions fit the slab layout
+  DevSlab<double> s_rows, s_cols;  // K by row (gathers v), K by column (gathers u_k)
+  int gc1k = 1, gc1d = 1, gc2 = 1;  // grids of the combine kernels
 };
+
+// slab.cu
+template <typename T>
+int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevSlab<T> *out);
+int slab_plan(plsqr_ctx *ctx);
+// plsqr_gpu.cu: partial-sum counts of the current product path
+int ctx_pu_k(const plsqr_ctx *ctx);
+int ctx_pu_d(const plsqr_ctx *ctx);
+int ctx_pv(const plsqr_ctx *ctx);
 
 void ctx_set_error(plsqr_ctx *ctx, const char *fmt, ...);
 int ctx_dev_alloc_bytes(plsqr_ctx *ctx, void **p, size_t bytes);

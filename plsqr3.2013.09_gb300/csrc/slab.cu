@@ -1,0 +1,125 @@
+// Construction of the slab layout (slab.cuh) on the device, at context
+// creation: count entries per (slab, line), lay the segments out slab-major
+// with 8-entry padding, scatter, and cut every slab's lines into
+// nonzero-balanced ranges, one per block.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "plsqr_internal.h"
+#include "slab.cuh"
+
+using namespace plsqr;
+
+#define CK(call)                                                               \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ctx_set_error(ctx, "%s:%d %s: %s", __FILE__, __LINE__, #call,            \
+                    cudaGetErrorString(e_));                                   \
+      return PLSQR_ERR_CUDA;                                                   \
+    }                                                                          \
+  } while (0)
+
+namespace {
+constexpr int kMaxSlabs = 64;  // k_slab_count / k_slab_fill keep one counter per slab
+}
+
+template <typename T>
+int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevSlab<T> *out) {
+  const int n_lines = L.n_lines;
+  const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
+  if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
+  int rc;
+  int64_t *cnt = nullptr;
+  const int64_t cells = (int64_t)n_slabs * n_lines;
+  if ((rc = dev_alloc(ctx, &cnt, (size_t)std::max<int64_t>(cells, 1)))) return rc;
+  const int g = std::max(1, std::min(ctx->sm_count * 8, (n_lines + 255) / 256));
+  k_slab_count<<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, n_lines, n_slabs, slab, cnt);
+  CK(cudaGetLastError());
+  std::vector<int64_t> hc((size_t)std::max<int64_t>(cells, 1));
+  CK(cudaMemcpyAsync(hc.data(), cnt, sizeof(int64_t) * cells, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, cnt);
+  // slab-major segment starts
+  std::vector<int64_t> sp((size_t)n_slabs * (n_lines + 1));
+  int64_t run = 0;
+  for (int s = 0; s < n_slabs; ++s) {
+    for (int l = 0; l < n_lines; ++l) {
+      sp[(size_t)s * (n_lines + 1) + l] = run;
+      run += hc[(size_t)s * n_lines + l];
+    }
+    sp[(size_t)s * (n_lines + 1) + n_lines] = run;
+  }
+  out->n_lines = n_lines;
+  out->n_slabs = n_slabs;
+  out->slab = slab;
+  out->n_idx = n_idx;
+  out->nnz_padded = run;
+  if ((rc = dev_alloc(ctx, &out->ptr, sp.size())) || (rc = dev_alloc(ctx, &out->idx, (size_t)run)) ||
+      (rc = dev_alloc(ctx, &out->val, (size_t)run)) ||
+      (rc = dev_alloc(ctx, &out->partial, (size_t)std::max<int64_t>(cells, 1))))
+    return rc;
+  CK(cudaMemcpy(out->ptr, sp.data(), sizeof(int64_t) * sp.size(), cudaMemcpyHostToDevice));
+  k_slab_fill<T><<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, L.val, n_lines, n_slabs, slab, out->ptr,
+                                             out->idx, out->val);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  // blocks per slab: about two waves of one resident block per SM in total
+  int bps = std::max(1, (2 * ctx->sm_count + n_slabs - 1) / n_slabs);
+  if (const char *e = getenv("PLSQR_SLAB_BLOCKS"))
+    if (atoi(e) > 0) bps = std::max(1, atoi(e) / n_slabs);
+  out->bps = bps;
+  std::vector<int32_t> lp((size_t)n_slabs * (bps + 1));
+  for (int s = 0; s < n_slabs; ++s) {
+    const int64_t *seg = sp.data() + (size_t)s * (n_lines + 1);
+    const int64_t b0 = seg[0], tot = seg[n_lines] - b0;
+    int32_t *o = lp.data() + (size_t)s * (bps + 1);
+    o[0] = 0;
+    for (int r = 1; r < bps; ++r) {
+      const int64_t target = b0 + (int64_t)((long double)tot * r / bps);
+      const int64_t *it = std::lower_bound(seg, seg + n_lines + 1, target);
+      o[r] = std::max<int32_t>(o[r - 1], (int32_t)std::min<int64_t>(it - seg, n_lines));
+    }
+    o[bps] = n_lines;
+  }
+  if ((rc = dev_alloc(ctx, &out->lpart, lp.size()))) return rc;
+  CK(cudaMemcpy(out->lpart, lp.data(), sizeof(int32_t) * lp.size(), cudaMemcpyHostToDevice));
+  // the launching translation unit sets the kernel's shared-memory limit
+  out->smem = sizeof(T) * (size_t)std::min(slab, n_idx);
+  return PLSQR_OK;
+}
+
+template int build_slab<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t, DevSlab<double> *);
+template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, DevSlab<float> *);
+
+// Plan the slab path: slab_ok when every dimension fits kMaxSlabs slabs of
+// 49,152 FP32 values (the mixed solver's inner products always use slabs
+// then).  The FP64 products use the per-line kernels unless PLSQR_SLABS=1
+// asks for FP64 slabs: measured on the 96x96x32 problem, splitting each line
+// into slab segments adds one warp reduction per segment on the FP64 pipe,
+// which costs more than the shared-memory gathers save.
+int slab_plan(plsqr_ctx *ctx) {
+  ctx->use_slabs = false;
+  const int fslab = 49152;
+  ctx->slab_ok = ctx->nnz_k > 0 && (ctx->n + fslab - 1) / fslab <= kMaxSlabs &&
+                 (ctx->m_k + fslab - 1) / fslab <= kMaxSlabs;
+  const int sm = ctx->sm_count, half = kMaxParts / 2;
+  ctx->gc1k = std::max(1, std::min({sm * 2, (ctx->m_k + 255) / 256, half}));
+  ctx->gc1d = std::max(1, std::min({sm * 2, (ctx->m_d + 255) / 256, half}));
+  ctx->gc2 = std::max(1, std::min({sm * 4, (ctx->n + 255) / 256, kMaxParts}));
+  const char *e = getenv("PLSQR_SLABS");
+  if (!e || atoi(e) != 1) return PLSQR_OK;
+  int slab = 24576;  // 192 KB of FP64 per block
+  if (const char *s = getenv("PLSQR_SLAB_SIZE"))
+    if (atoi(s) >= 1024 && atoi(s) <= 28672) slab = atoi(s);
+  const int ns_r = (ctx->n + slab - 1) / slab, ns_c = (ctx->m_k + slab - 1) / slab;
+  if (ns_r > kMaxSlabs || ns_c > kMaxSlabs || ctx->nnz_k == 0) return PLSQR_OK;
+  int rc;
+  if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, &ctx->s_rows)) ||
+      (rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, &ctx->s_cols)))
+    return rc;
+  ctx->use_slabs = true;
+  return PLSQR_OK;
+}

@@ -1,0 +1,211 @@
+// Slab layout of the kernel matrix and the products built on it.
+//
+// A product gathers a vector (v for A x, u_k for A^T y) at the matrix's
+// indices.  The index space is cut into slabs of S entries that fit in shared
+// memory (S = 24,576 FP64 values = 192 KB).  Every line (row for A x, column
+// for A^T y) is stored slab by slab: the entries of line l whose index falls
+// in slab s form the segment (s, l), with a 16-bit slab-local index, padded
+// with zero entries to a multiple of 8 so that a lane loads 8 indices and their
+// values with 16-byte loads.  Segments are stored slab-major:
+//
+//   ptr[s * (n_lines + 1) + l]   start of segment (s, l) in idx / val
+//   idx[e]  uint16, val[e]  T    entries (10 bytes per FP64 nonzero, 6 per FP32)
+//
+// k_slab_spmv: block b works on slab s = b / B: it copies x[s*S, (s+1)*S) into
+// shared memory once, then its warps stream the segments of a contiguous,
+// nonzero-balanced range of lines and write partial[s][l].  The gathers hit
+// shared memory instead of scattering over L2.  k_combine_rows /
+// k_combine_cols add the partials of the slabs in slab order (so results are
+// deterministic), add the damping part, apply the LSQR scale and write the
+// per-block sums of squares the norm kernels finish.
+#pragma once
+
+#include "kernels_fp64.cuh"
+
+namespace plsqr {
+
+template <typename T>
+struct SlabCsr {
+  const int64_t *ptr;   // [n_slabs * (n_lines + 1)]
+  const uint16_t *idx;  // slab-local indices
+  const T *val;
+  int32_t n_lines;      // lines (rows for A x, columns for A^T y)
+  int32_t n_slabs;
+  int32_t slab;         // S
+  int32_t n_idx;        // length of the gathered vector
+};
+
+// ---- construction (setup only) --------------------------------------------
+
+// cnt[s * n_lines + l] = entries of line l in slab s, rounded up to 8.
+static __global__ void k_slab_count(const int64_t *__restrict__ ptr, const int32_t *__restrict__ idx,
+                                    int n_lines, int n_slabs, int slab, int64_t *__restrict__ cnt) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n_lines; l += gridDim.x * blockDim.x) {
+    int64_t c[64];
+    for (int s = 0; s < n_slabs; ++s) c[s] = 0;
+    for (int64_t e = ptr[l]; e < ptr[l + 1]; ++e) c[idx[e] / slab]++;
+    for (int s = 0; s < n_slabs; ++s) cnt[(int64_t)s * n_lines + l] = (c[s] + 7) & ~int64_t(7);
+  }
+}
+
+// Scatter line l's entries into its segments; pad with (index 0, value 0).
+template <typename T>
+__global__ void k_slab_fill(const int64_t *__restrict__ ptr, const int32_t *__restrict__ idx,
+                            const double *__restrict__ val, int n_lines, int n_slabs, int slab,
+                            const int64_t *__restrict__ sptr, uint16_t *__restrict__ sidx,
+                            T *__restrict__ sval) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n_lines; l += gridDim.x * blockDim.x) {
+    int64_t cur[64];
+    for (int s = 0; s < n_slabs; ++s) cur[s] = sptr[(int64_t)s * (n_lines + 1) + l];
+    for (int64_t e = ptr[l]; e < ptr[l + 1]; ++e) {
+      const int s = idx[e] / slab;
+      const int64_t o = cur[s]++;
+      sidx[o] = (uint16_t)(idx[e] - s * slab);
+      sval[o] = (T)val[e];
+    }
+    for (int s = 0; s < n_slabs; ++s) {
+      const int64_t end = sptr[(int64_t)s * (n_lines + 1) + l + 1];
+      for (int64_t o = cur[s]; o < end; ++o) {
+        sidx[o] = 0;
+        sval[o] = (T)0;
+      }
+    }
+  }
+}
+
+// ---- products -----------------------------------------------------------------
+
+__device__ __forceinline__ void load8(const double *v, int64_t g, double (&o)[8]) {
+  const double2 *p = reinterpret_cast<const double2 *>(v) + 4 * g;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const double2 a = __ldg(p + j);
+    o[2 * j] = a.x;
+    o[2 * j + 1] = a.y;
+  }
+}
+__device__ __forceinline__ void load8(const float *v, int64_t g, float (&o)[8]) {
+  const float4 *p = reinterpret_cast<const float4 *>(v) + 2 * g;
+  const float4 a = __ldg(p), b = __ldg(p + 1);
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = a.z;
+  o[3] = a.w;
+  o[4] = b.x;
+  o[5] = b.y;
+  o[6] = b.z;
+  o[7] = b.w;
+}
+
+// partial[s * n_lines + l] = sum over segment (s, l) of val * x_slab[idx].
+// Blocks are slab-major: slab s = blockIdx.x / bps, range r = blockIdx.x % bps;
+// lpart[s * (bps + 1) + r] .. [.. + 1] is the range's first and end line.
+template <typename T, int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_slab_spmv(SlabCsr<T> A, const int32_t *__restrict__ lpart, int bps, const T *__restrict__ x,
+                T *__restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *xs = reinterpret_cast<T *>(smem_raw);
+  const int s = blockIdx.x / bps, r = blockIdx.x - s * bps;
+  const int64_t base = (int64_t)s * A.slab;
+  const int len = (int)min((int64_t)A.slab, (int64_t)A.n_idx - base);
+  for (int i = threadIdx.x; i < len; i += kThreads) xs[i] = x[base + i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t *ptr = A.ptr + (int64_t)s * (A.n_lines + 1);
+  const int l1 = lpart[s * (bps + 1) + r + 1];
+  const uint4 *idx8 = reinterpret_cast<const uint4 *>(A.idx);
+  for (int l = lpart[s * (bps + 1) + r] + (threadIdx.x >> 5); l < l1; l += kThreads / 32) {
+    const int64_t g0 = ptr[l] >> 3, g1 = ptr[l + 1] >> 3;  // groups of 8 entries
+    T acc0 = 0, acc1 = 0;
+    for (int64_t g = g0 + lane; g < g1; g += 32) {
+      const uint4 q = __ldg(idx8 + g);
+      T v[8];
+      load8(A.val, g, v);
+      acc0 = fmaT(v[0], xs[q.x & 0xffff], acc0);
+      acc1 = fmaT(v[1], xs[q.x >> 16], acc1);
+      acc0 = fmaT(v[2], xs[q.y & 0xffff], acc0);
+      acc1 = fmaT(v[3], xs[q.y >> 16], acc1);
+      acc0 = fmaT(v[4], xs[q.z & 0xffff], acc0);
+      acc1 = fmaT(v[5], xs[q.z >> 16], acc1);
+      acc0 = fmaT(v[6], xs[q.w & 0xffff], acc0);
+      acc1 = fmaT(v[7], xs[q.w >> 16], acc1);
+    }
+    const T t = warp_sum(acc0 + acc1);
+    if (lane == 0) partial[(int64_t)s * A.n_lines + l] = t;
+  }
+}
+
+// u_k[r] = scale*u_k[r] + sum_s partial[s][r] (blocks [0, gk)); u_d[r] =
+// scale*u_d[r] + (D v)[r] (blocks [gk, grid)); per-block sums of squares.
+template <typename T, int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_combine_rows(const T *__restrict__ partial, int n_slabs, int m_k, Csr D,
+                   const T *__restrict__ v, T *__restrict__ u, int gk, int mode,
+                   const DevState *__restrict__ st, double *__restrict__ parts) {
+  __shared__ double smem[kThreads / 32];
+  double s = 1.0;
+  if (mode == kScaleNegAlpha) s = -st->alpha;
+  double sq = 0.0;
+  if ((int)blockIdx.x < gk) {
+    for (int r = blockIdx.x * kThreads + threadIdx.x; r < m_k; r += gk * kThreads) {
+      T t = 0;
+      for (int q = 0; q < n_slabs; ++q) t += partial[(int64_t)q * m_k + r];
+      const T y = scaled_add(s, u[r], t);
+      u[r] = y;
+      sq = fma((double)y, (double)y, sq);
+    }
+  } else {
+    const int gd = gridDim.x - gk;
+    T *ud = u + m_k;
+    for (int r = (blockIdx.x - gk) * kThreads + threadIdx.x; r < D.n_lines; r += gd * kThreads) {
+      const T y = scaled_add(s, ud[r], damp_row(D, v, r));
+      ud[r] = y;
+      sq = fma((double)y, (double)y, sq);
+    }
+  }
+  const double b = block_sum<kThreads>(sq, smem);
+  if (threadIdx.x == 0 && parts) parts[blockIdx.x] = b;
+}
+
+// Damping column c times u_d in stored order (FP64: mul and add rounded apart
+// as in CPUSpMV.c:270-275).
+__device__ __forceinline__ double damp_col(const Csr &DC, const double *__restrict__ ud, int c) {
+  return seq_dot_f64(DC.idx, DC.val, ud, DC.ptr[c], DC.ptr[c + 1]);
+}
+__device__ __forceinline__ float damp_col(const Csr &DC, const float *__restrict__ ud, int c) {
+  float t = 0.f;
+  for (int64_t e = DC.ptr[c]; e < DC.ptr[c + 1]; ++e) t = fmaf((float)DC.val[e], ud[DC.idx[e]], t);
+  return t;
+}
+
+// v[c] = scale*v[c] + (sum_s partial[s][c] + (D^T u_d)[c]); per-block sums
+// of squares.  LSQR mode: skipped when beta == 0 (source/lsqr.c:530).
+template <typename T, int kThreads>
+__global__ void __launch_bounds__(kThreads)
+    k_combine_cols(const T *__restrict__ partial, int n_slabs, int n, Csr DC,
+                   const T *__restrict__ u, int m_k, T *__restrict__ v, int mode,
+                   const DevState *__restrict__ st, double *__restrict__ parts) {
+  __shared__ double smem[kThreads / 32];
+  double s = 1.0;
+  if (mode == kScaleNegBeta) {
+    if (!st->s_beta_pos) return;
+    s = -st->beta;
+  } else if (mode == kScaleZero) {
+    if (!st->s_beta_pos) return;
+    s = 0.0;
+  }
+  const T *ud = u + m_k;
+  double sq = 0.0;
+  for (int c = blockIdx.x * kThreads + threadIdx.x; c < n; c += gridDim.x * kThreads) {
+    T t = 0;
+    for (int q = 0; q < n_slabs; ++q) t += partial[(int64_t)q * n + c];
+    const T y = scaled_add(s, v[c], t + damp_col(DC, ud, c));  // x += (s_k + s_d)
+    v[c] = y;
+    sq = fma((double)y, (double)y, sq);
+  }
+  const double b = block_sum<kThreads>(sq, smem);
+  if (threadIdx.x == 0 && parts) parts[blockIdx.x] = b;
+}
+
+}  // namespace plsqr

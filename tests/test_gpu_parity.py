@@ -121,6 +121,13 @@ def test_adjoint_identity(pkg, problems):
     assert abs(lhs - rhs) <= 1e-12 * (np.abs(ax_k) @ np.abs(yk) + np.abs(ax_d) @ np.abs(yd))
 
 
+def test_visit_order_changes_only_rounding(pkg, problems):
+    prob = problems("grid32")
+    with pkg.Context(prob) as c1, pkg.Context(prob, grid=(0, 0, 0)) as c2:
+        a, b = c1.lsqr(lsqr_iteration=60), c2.lsqr(lsqr_iteration=60)
+    assert rel(a["x"], b["x"]) <= 1e-12
+
+
 def test_graph_replay_equals_stream_launch_and_is_deterministic(pkg, problems):
     prob = problems("grid32")
     outs = []
@@ -139,7 +146,8 @@ def test_context_from_files_equals_context_from_arrays(pkg, problems):
     with pkg.Context(files=files) as c1:
         a = c1.lsqr(lsqr_iteration=it)
         assert np.array_equal(c1.get_b(), problems("tiny").b_k)
-    with pkg.Context(problems("tiny")) as c2:
+    # same column visit order as the file-loaded context (no grid known)
+    with pkg.Context(problems("tiny"), grid=(0, 0, 0)) as c2:
         b = c2.lsqr(lsqr_iteration=it)
     assert np.array_equal(a["x"], b["x"])
     assert rel(a["x"], g["x"]) <= LSQR_TOL
