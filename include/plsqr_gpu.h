@@ -203,6 +203,27 @@ int plsqr_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch)
  * preceding plsqr_lsqr on the context (state and history are overwritten). */
 int plsqr_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration);
 
+/* ---- product without device allocation ----------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory: code running inside CUDA stream capture (cudaMalloc is not allowed
+ * there), code whose device memory belongs to another allocator or a fixed
+ * budget, and callers that cannot block on the driver's allocator.
+ * y <- y + A x for an n_rows-row CSR matrix (row_ptr int64[n_rows+1],
+ * col_idx/val 16-byte aligned, indices in range of x) and *nrm2 = ||y||_2
+ * after the update; every pointer is device memory, the work is ordered on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream) and nothing is
+ * synchronised.  It allocates no memory: its per-block partial sums live in a
+ * 128 KB static device array of the library (held by every GPU that loads the
+ * library until exit), so n_rows is limited to PLSQR_NOALLOC_MAX_ROWS
+ * (PLSQR_ERR_ARG beyond it).  The first call on a device looks up that array
+ * and should come before any stream capture; calls share the array, so calls
+ * that overlap on the GPU race. */
+#define PLSQR_NOALLOC_MAX_ROWS 1048576
+int plsqr_aprod1_nrm2_noalloc(int32_t n_rows, const int64_t *row_ptr,
+                              const int32_t *col_idx, const double *val,
+                              const double *x, double *y, double *nrm2,
+                              void *stream);
+
 /* ---- files, host side (no GPU needed) ----------------------------------- */
 /* read_kernel_col_info (plsqr3.c:1379-1409): nnz[n], start[n] (0-based,
  * -1 where the file has 0) and the total. */

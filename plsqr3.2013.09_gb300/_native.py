@@ -21,6 +21,7 @@ ERR = {
     -9: "PLSQR_ERR_INTERNAL", -10: "PLSQR_ERR_NUMERIC",
 }
 PREC_FP64, PREC_MIXED = 0, 1
+NOALLOC_MAX_ROWS = 1048576  # PLSQR_NOALLOC_MAX_ROWS
 
 vp = C.c_void_p
 i32, i64, f64, u64 = C.c_int32, C.c_int64, C.c_double, C.c_uint64
@@ -98,6 +99,7 @@ SIGNATURES = {
     "plsqr_write_result": (C.c_int, [vp, C.c_char_p]),
     "plsqr_bench_aprod": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(f64)]),
     "plsqr_bench_iteration": (C.c_int, [vp, C.c_int, C.POINTER(f64)]),
+    "plsqr_aprod1_nrm2_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "plsqr_io_read_kernel_info": (C.c_int, [C.c_char_p, i32, vp, vp, C.POINTER(i64)]),
     "plsqr_io_read_kernel": (C.c_int, [C.c_char_p, C.c_char_p, i32, i32, vp, vp, vp]),
     "plsqr_io_read_int32_counts": (C.c_int, [C.c_char_p, i64, vp, C.POINTER(i64)]),
