@@ -127,7 +127,11 @@ typedef struct {
   double anorm, acond, rnorm, arnorm_out, xnorm;
   double arnorm, bnorm, dxmax;
   int32_t maxdx, pad;
-  double seconds; /* device time of the iteration loop (CUDA events) */
+  double seconds;       /* device time of the iteration loop (CUDA events), the
+                           region of the reference's "Parallel LSQR time"
+                           (source/lsqr.c:476-842)                            */
+  double seconds_total; /* device time from the start-up's first kernel to the
+                           end of the loop (mixed precision: the whole solve)  */
 } plsqr_result;
 
 typedef struct plsqr_ctx plsqr_ctx;

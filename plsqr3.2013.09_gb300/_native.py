@@ -59,7 +59,8 @@ class LsqrArgs(C.Structure):
 class Result(C.Structure):
     _fields_ = [("istop", i32), ("itn", i32), ("anorm", f64), ("acond", f64), ("rnorm", f64),
                 ("arnorm_out", f64), ("xnorm", f64), ("arnorm", f64), ("bnorm", f64),
-                ("dxmax", f64), ("maxdx", i32), ("pad", i32), ("seconds", f64)]
+                ("dxmax", f64), ("maxdx", i32), ("pad", i32), ("seconds", f64),
+                ("seconds_total", f64)]
 
 
 class SynthParams(C.Structure):

@@ -225,10 +225,11 @@ __global__ void __launch_bounds__(kThreads)
 __device__ __forceinline__ double scale_elem(double x, double r) { return dmul(x, r); }
 __device__ __forceinline__ float scale_elem(float x, double r) { return x * (float)r; }
 
+// mirror (optional): FP32 copy of the scaled u, gathered by FP32 products.
 template <typename T, int kThreads>
 __global__ void __launch_bounds__(kThreads)
     k_norm_u(T *__restrict__ u, int64_t m, const double *__restrict__ parts, int gk, int gd,
-             DevState *__restrict__ st, int start) {
+             DevState *__restrict__ st, int start, float *__restrict__ mirror = nullptr) {
   __shared__ double smem[kThreads / 32];
   __shared__ double s_rb;
   const double sk = sum_parts<kThreads>(parts, gk, smem);
@@ -250,8 +251,11 @@ __global__ void __launch_bounds__(kThreads)
   const double rb = s_rb;
   if (rb == 0.0) return;  // beta == 0: u is left as is
   for (int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x; i < m;
-       i += (int64_t)gridDim.x * kThreads)
-    u[i] = scale_elem(u[i], rb);
+       i += (int64_t)gridDim.x * kThreads) {
+    const T y = scale_elem(u[i], rb);
+    u[i] = y;
+    if (mirror) mirror[i] = (float)y;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -310,7 +314,8 @@ __global__ void __launch_bounds__(kThreads)
                double *__restrict__ se, const double *__restrict__ xref, int n,
                const double *__restrict__ parts, int gp, DevState *__restrict__ st,
                double *__restrict__ parts_dk, double *__restrict__ parts_err,
-               plsqr_iter *__restrict__ hist, int start) {
+               plsqr_iter *__restrict__ hist, int start, float *__restrict__ v_mirror = nullptr,
+               const double *__restrict__ x_base = nullptr) {
   __shared__ double smem[kThreads / 32];
   __shared__ double s_alpha, s_ra;
   __shared__ Step s_step;
@@ -331,6 +336,7 @@ __global__ void __launch_bounds__(kThreads)
       double vi = v[i];
       if (ra != 0.0) vi = dmul(vi, ra);
       v[i] = vi;
+      if (v_mirror) v_mirror[i] = (float)vi;
       w[i] = ra != 0.0 ? vi : 0.0;  // w = v only when alpha > 0 (lsqr.c:392-395)
       x[i] = 0.0;
       if (se) se[i] = 0.0;
@@ -371,6 +377,7 @@ __global__ void __launch_bounds__(kThreads)
       vi = dmul(vi, ra);
       v[i] = vi;
     }
+    if (v_mirror) v_mirror[i] = (float)vi;
     const double t = w[i];
     const double xi = dadd(dmul(sp.t1, t), x[i]);
     x[i] = xi;
@@ -379,7 +386,7 @@ __global__ void __launch_bounds__(kThreads)
     if (se) se[i] = dadd(tt, se[i]);
     dk += tt;
     if (xref) {
-      const double d = xi - xref[i];
+      const double d = (x_base ? x_base[i] + xi : xi) - xref[i];
       e2 = fma(d, d, e2);
     }
   }

@@ -34,6 +34,8 @@ struct MixedState {
   bool slabs = false;
   DevSlab<float> s_rows, s_cols;
   float *uf = nullptr, *vf = nullptr, *wf = nullptr, *dxf = nullptr;
+  double *dx = nullptr;  // FP64 correction of the FP64-vector inner sweeps
+  bool v64 = false;      // inner sweeps keep u, v, w, dx in FP64 (slab products in FP32)
   double *b = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_key = -1;
@@ -68,7 +70,7 @@ int mixed_prepare(plsqr_ctx *ctx) {
       (rc = dev_alloc(ctx, &M->kc_hi, (size_t)ctx->nnz_k)) ||
       (rc = dev_alloc(ctx, &M->uf, (size_t)m)) || (rc = dev_alloc(ctx, &M->vf, (size_t)ctx->n)) ||
       (rc = dev_alloc(ctx, &M->wf, (size_t)ctx->n)) ||
-      (rc = dev_alloc(ctx, &M->dxf, (size_t)ctx->n)) ||
+      (rc = dev_alloc(ctx, &M->dxf, (size_t)ctx->n)) || (rc = dev_alloc(ctx, &M->dx, (size_t)ctx->n)) ||
       (rc = dev_alloc(ctx, &M->b, (size_t)std::max(ctx->m_k, 1))))
     return rc;
   const int g = ctx->sm_count * 8;
@@ -77,13 +79,16 @@ int mixed_prepare(plsqr_ctx *ctx) {
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->slab_ok) {
-    const int slab = 49152;  // 192 KB of FP32 per block
-    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, &M->s_rows)) ||
-        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, &M->s_cols)))
+    int slab = 24576;  // 96 KB of FP32 per block: two blocks per SM
+    if (const char *e = getenv("PLSQR_SLAB_SIZE_F"))
+      if (atoi(e) >= 1024 && atoi(e) <= 57344) slab = atoi(e);
+    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 8 * ctx->sm_count, &M->s_rows)) ||
+        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 8 * ctx->sm_count, &M->s_cols)))
       return rc;
-    CK(cudaFuncSetAttribute(k_slab_spmv<float, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)std::max(M->s_rows.smem, M->s_cols.smem)));
+    if ((rc = slab_set_smem<float>(std::max(M->s_rows.smem, M->s_cols.smem)))) return rc;
     M->slabs = true;
+    const char *e = getenv("PLSQR_MIXED_F32VEC");
+    M->v64 = !(e && atoi(e) == 1);
   }
   return PLSQR_OK;
 }
@@ -104,16 +109,12 @@ static CsrT<float> cols_f(const plsqr_ctx *ctx) {
 }
 // the inner sweeps' products: the FP64 kernels instantiated for FP32, on the
 // FP32 slabs when present
-static SlabCsr<float> view(const DevSlab<float> &S) {
-  return SlabCsr<float>{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx};
-}
 static void m1f(plsqr_ctx *ctx, cudaStream_t s) {
   MixedState *M = ctx->mixed;
   if (M->slabs) {
     const DevSlab<float> &S = M->s_rows;
-    k_slab_spmv<float, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(view(S), S.lpart, S.bps, M->vf,
-                                                                     S.partial);
-    k_combine_rows<float, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
+    slab_spmv(S, ctx->slab_group_f, M->vf, s);
+    k_combine_rows<float, float, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
         S.partial, S.n_slabs, ctx->m_k, ctx->D.csr(), M->vf, M->uf, ctx->gc1k, kScaleNegAlpha,
         ctx->st, ctx->parts_u);
     return;
@@ -126,9 +127,8 @@ static void m2f(plsqr_ctx *ctx, cudaStream_t s, int mode) {
   MixedState *M = ctx->mixed;
   if (M->slabs) {
     const DevSlab<float> &S = M->s_cols;
-    k_slab_spmv<float, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(view(S), S.lpart, S.bps, M->uf,
-                                                                     S.partial);
-    k_combine_cols<float, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+    slab_spmv(S, ctx->slab_group_f, M->uf, s);
+    k_combine_cols<float, float, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
         S.partial, S.n_slabs, ctx->n, ctx->DC.csr(), M->uf, ctx->m_k, M->vf, mode, ctx->st,
         ctx->parts_v);
     return;
@@ -138,7 +138,48 @@ static void m2f(plsqr_ctx *ctx, cudaStream_t s, int mode) {
       ctx->parts_v);
 }
 
+// FP64-vector inner sweeps: the products read the FP32 mirrors of v and u
+// (written by the scaling kernels) with the FP32 slab matrix and combine the
+// FP32 partials into the FP64 vectors.
+static void m1v(plsqr_ctx *ctx, cudaStream_t s, int mode) {
+  MixedState *M = ctx->mixed;
+  slab_spmv(M->s_rows, ctx->slab_group_f, M->vf, s);
+  k_combine_rows<float, double, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
+      M->s_rows.partial, M->s_rows.n_slabs, ctx->m_k, ctx->D.csr(), ctx->v, ctx->u, ctx->gc1k,
+      mode, ctx->st, ctx->parts_u);
+}
+static void m2v(plsqr_ctx *ctx, cudaStream_t s, int mode) {
+  MixedState *M = ctx->mixed;
+  slab_spmv(M->s_cols, ctx->slab_group_f, M->uf, s);
+  k_combine_cols<float, double, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+      M->s_cols.partial, M->s_cols.n_slabs, ctx->n, ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, mode,
+      ctx->st, ctx->parts_v);
+}
+
+static int enqueue_inner64(plsqr_ctx *ctx, cudaStream_t s) {
+  MixedState *M = ctx->mixed;
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  const double *xref = ctx->has_ref ? ctx->xref : nullptr;
+  m1v(ctx, s, kScaleNegAlpha);
+  k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->parts_u, ctx->gc1k,
+                                                           ctx->gc1d, ctx->st, 0, M->uf);
+  m2v(ctx, s, kScaleNegBeta);
+  k_update_x<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
+      ctx->v, ctx->w, M->dx, nullptr, xref, ctx->n, ctx->parts_v, ctx->gc2, ctx->st, ctx->parts_dk,
+      xref ? ctx->parts_err : nullptr, ctx->hist, 0, M->vf, ctx->x);
+  k_tail<kThreads><<<1, kThreads, 0, s>>>(ctx->st, ctx->parts_dk, xref ? ctx->parts_err : nullptr,
+                                           ctx->gvx, ctx->x, ctx->hist);
+  CK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
+static __global__ void k_add_vec(double *__restrict__ x, const double *__restrict__ dx, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] += dx[i];
+}
+
 static int enqueue_inner(plsqr_ctx *ctx, cudaStream_t s) {
+  if (ctx->mixed->v64) return enqueue_inner64(ctx, s);
   MixedState *M = ctx->mixed;
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   const double *xref = ctx->has_ref ? ctx->xref : nullptr;
@@ -157,7 +198,7 @@ static int enqueue_inner(plsqr_ctx *ctx, cudaStream_t s) {
 
 static int ensure_inner_graph(plsqr_ctx *ctx) {
   MixedState *M = ctx->mixed;
-  const int key = ctx->has_ref ? 1 : 0;
+  const int key = (ctx->has_ref ? 1 : 0) | (M->v64 ? 2 : 0);
   if (M->graph && M->graph_key == key && M->graph_hist == ctx->hist) return PLSQR_OK;
   if (M->graph) cudaGraphExecDestroy(M->graph);
   M->graph = nullptr;
@@ -227,13 +268,24 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     // outer residual and the start-up of the inner solve
     k_residual<kThreads><<<ctx->g1k + ctx->g1d, kThreads, 0, ctx->stream>>>(
         rows_hilo(ctx), ctx->D.csr(), ctx->kpart, ctx->x, M->b, ctx->u, ctx->g1k, ctx->parts_u);
-    k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(
-        ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d, ctx->st, 1);
-    k_to_f32<<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, M->uf);
-    m2f(ctx, ctx->stream, kScaleZero);
-    k_update_dx_f32<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
-        M->vf, M->wf, M->dxf, ctx->x, nullptr, ctx->n, ctx->parts_v, pv(ctx), ctx->st,
-        ctx->parts_dk, nullptr, 1);
+    if (M->v64) {
+      // FP64-vector inner solve: scaled r and its FP32 mirror, v = A^T u
+      k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(
+          ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d, ctx->st, 1, M->uf);
+      CK(cudaMemsetAsync(ctx->v, 0, sizeof(double) * ctx->n, ctx->stream));
+      m2v(ctx, ctx->stream, kScaleZero);
+      k_update_x<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
+          ctx->v, ctx->w, M->dx, nullptr, nullptr, ctx->n, ctx->parts_v, ctx->gc2, ctx->st,
+          ctx->parts_dk, nullptr, nullptr, 1, M->vf, nullptr);
+    } else {
+      k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(
+          ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d, ctx->st, 1);
+      k_to_f32<<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, M->uf);
+      m2f(ctx, ctx->stream, kScaleZero);
+      k_update_dx_f32<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
+          M->vf, M->wf, M->dxf, ctx->x, nullptr, ctx->n, ctx->parts_v, pv(ctx), ctx->st,
+          ctx->parts_dk, nullptr, 1);
+    }
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -249,7 +301,10 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     }
     if (cur.done) break;  // A^T r = 0: x is a least-squares solution
     for (int i = 0; i < I; ++i) CK(cudaGraphLaunch(M->graph, ctx->stream));
-    k_add_dx<<<ctx->gvx, kThreads, 0, ctx->stream>>>(ctx->x, M->dxf, ctx->n);
+    if (M->v64)
+      k_add_vec<<<ctx->gvx, kThreads, 0, ctx->stream>>>(ctx->x, M->dx, ctx->n);
+    else
+      k_add_dx<<<ctx->gvx, kThreads, 0, ctx->stream>>>(ctx->x, M->dxf, ctx->n);
     CK(cudaGetLastError());
     done_sweeps = s + 1;
     last_itn = (s + 1) * I;
@@ -279,6 +334,7 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   r.dxmax = cur.dxmax;
   r.maxdx = cur.maxdx;
   r.seconds = ms * 1e-3;
+  r.seconds_total = r.seconds;
   if (res) *res = r;
   if (hist) memcpy(hist, hh.data(), sizeof(plsqr_iter) * (total + 1));
   return PLSQR_OK;
@@ -288,8 +344,13 @@ int mixed_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch)
   int rc;
   if ((rc = mixed_prepare(ctx))) return rc;
   CK(cudaSetDevice(ctx->opts.device));
+  const bool v64 = ctx->mixed->v64;
   auto launch = [&]() {
-    if (mode == 1)
+    if (v64 && mode == 1)
+      m1v(ctx, ctx->stream, kScaleOne);
+    else if (v64)
+      m2v(ctx, ctx->stream, kScaleZero);
+    else if (mode == 1)
       m1f(ctx, ctx->stream);
     else
       m2f(ctx, ctx->stream, kScaleZero);

@@ -189,13 +189,40 @@ static void launch_m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
 // combine kernel (scale, damping part, sums of squares).  Otherwise the
 // per-line kernels.  Either way `parts` receives pu_k + pu_d (mode 1) or pv
 // (mode 2) per-block sums of squares for the norm kernels.
+template <typename T>
+void slab_spmv(const DevSlab<T> &S, int group, const T *x, cudaStream_t s) {
+  const SlabCsr<T> A{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx};
+  const int grid = S.n_slabs * S.bps;
+  if (group == 4)
+    k_slab_spmv<T, 1024, 4><<<grid, 1024, S.smem, s>>>(A, S.lpart, S.bps, x, S.partial);
+  else if (group == 8)
+    k_slab_spmv<T, 1024, 8><<<grid, 1024, S.smem, s>>>(A, S.lpart, S.bps, x, S.partial);
+  else if (group == 32)
+    k_slab_spmv<T, 1024, 32><<<grid, 1024, S.smem, s>>>(A, S.lpart, S.bps, x, S.partial);
+  else
+    k_slab_spmv<T, 1024, 16><<<grid, 1024, S.smem, s>>>(A, S.lpart, S.bps, x, S.partial);
+}
+template void slab_spmv<double>(const DevSlab<double> &, int, const double *, cudaStream_t);
+template void slab_spmv<float>(const DevSlab<float> &, int, const float *, cudaStream_t);
+
+template <typename T>
+int slab_set_smem(size_t smem) {
+  const int b = (int)std::max<size_t>(smem, 1);
+  if (cudaFuncSetAttribute(k_slab_spmv<T, 1024, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
+      cudaFuncSetAttribute(k_slab_spmv<T, 1024, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
+      cudaFuncSetAttribute(k_slab_spmv<T, 1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
+      cudaFuncSetAttribute(k_slab_spmv<T, 1024, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
+    return PLSQR_ERR_CUDA;
+  return PLSQR_OK;
+}
+template int slab_set_smem<double>(size_t);
+template int slab_set_smem<float>(size_t);
+
 static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
-  if (ctx->use_slabs) {
+  if (ctx->use_slabs_rows) {
     const DevSlab<double> &S = ctx->s_rows;
-    k_slab_spmv<double, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(
-        SlabCsr<double>{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx}, S.lpart, S.bps,
-        ctx->v, S.partial);
-    k_combine_rows<double, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
+    slab_spmv(S, ctx->slab_group, ctx->v, s);
+    k_combine_rows<double, double, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
         S.partial, S.n_slabs, ctx->m_k, ctx->D.csr(), ctx->v, ctx->u, ctx->gc1k, mode, ctx->st, parts);
     return;
   }
@@ -208,10 +235,8 @@ static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
 static void m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
   if (ctx->use_slabs) {
     const DevSlab<double> &S = ctx->s_cols;
-    k_slab_spmv<double, 1024><<<S.n_slabs * S.bps, 1024, S.smem, s>>>(
-        SlabCsr<double>{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx}, S.lpart, S.bps,
-        ctx->u, S.partial);
-    k_combine_cols<double, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+    slab_spmv(S, ctx->slab_group, ctx->u, s);
+    k_combine_cols<double, double, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
         S.partial, S.n_slabs, ctx->n, ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, mode, ctx->st, parts);
     return;
   }
@@ -224,16 +249,15 @@ static void m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
 // The slab kernel stages up to 192 KB of shared memory; the limit is a
 // per-module attribute, so it is set here, where the kernel is launched.
 static int slab_attrs(plsqr_ctx *ctx) {
-  if (!ctx->use_slabs) return PLSQR_OK;
-  const size_t smem = std::max(ctx->s_rows.smem, ctx->s_cols.smem);
-  CK(cudaFuncSetAttribute(k_slab_spmv<double, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)smem));
-  return PLSQR_OK;
+  if (!ctx->use_slabs && !ctx->use_slabs_rows) return PLSQR_OK;
+  const int rc = slab_set_smem<double>(std::max(ctx->s_rows.smem, ctx->s_cols.smem));
+  if (rc) ctx_set_error(ctx, "cudaFuncSetAttribute failed for the slab kernels");
+  return rc;
 }
 
 // partial-sum counts the norm kernels read
-int ctx_pu_k(const plsqr_ctx *ctx) { return ctx->use_slabs ? ctx->gc1k : ctx->g1k; }
-int ctx_pu_d(const plsqr_ctx *ctx) { return ctx->use_slabs ? ctx->gc1d : ctx->g1d; }
+int ctx_pu_k(const plsqr_ctx *ctx) { return ctx->use_slabs_rows ? ctx->gc1k : ctx->g1k; }
+int ctx_pu_d(const plsqr_ctx *ctx) { return ctx->use_slabs_rows ? ctx->gc1d : ctx->g1d; }
 int ctx_pv(const plsqr_ctx *ctx) { return ctx->use_slabs ? ctx->gc2 : ctx->g2; }
 
 // Spread the low 10 bits of v to every third bit.
@@ -325,6 +349,7 @@ static int ctx_init_common(plsqr_ctx *ctx) {
   CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   CK(cudaEventCreate(&ctx->ev0));
   CK(cudaEventCreate(&ctx->ev1));
+  CK(cudaEventCreate(&ctx->ev_start));
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, ctx->opts.device));
   ctx->sm_count = prop.multiProcessorCount;
@@ -332,6 +357,14 @@ static int ctx_init_common(plsqr_ctx *ctx) {
   const char *env = getenv("PLSQR_BLOCKS_PER_SM");
   if (env && atoi(env) > 0) ctx->blocks_per_sm = atoi(env);
   ctx->m2_blocks_per_sm = 48;
+  ctx->slab_group = 8;
+  env = getenv("PLSQR_SLAB_GROUP");
+  if (env && (atoi(env) == 4 || atoi(env) == 8 || atoi(env) == 16 || atoi(env) == 32))
+    ctx->slab_group = atoi(env);
+  ctx->slab_group_f = 16;
+  env = getenv("PLSQR_SLAB_GROUP_F");
+  if (env && (atoi(env) == 4 || atoi(env) == 8 || atoi(env) == 16 || atoi(env) == 32))
+    ctx->slab_group_f = atoi(env);
   ctx->unroll = 2;
   env = getenv("PLSQR_UNROLL");
   if (env && (atoi(env) == 1 || atoi(env) == 2 || atoi(env) == 4)) ctx->unroll = atoi(env);
@@ -423,6 +456,7 @@ void plsqr_ctx_destroy(plsqr_ctx *ctx) {
   ctx->allocs.clear();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -682,6 +716,7 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   if (ctx->has_ref) k_ref_norm<kThreads><<<1, kThreads, 0, ctx->stream>>>(ctx->xref, ctx->n, ctx->st);
 
   // start-up: beta u = b, alpha v = A^T u (lsqr.c:343-445)
+  CK(cudaEventRecord(ctx->ev_start, ctx->stream));
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   k_sumsq_u<kThreads><<<ctx->gsk + ctx->gsd, kThreads, 0, ctx->stream>>>(ctx->u, ctx->m_k, ctx->m_d,
                                                                           ctx->gsk, ctx->parts_u);
@@ -697,7 +732,7 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   CK(cudaStreamSynchronize(ctx->stream));
 
   int done_itn = 0;
-  float ms = 0.f;
+  float ms = 0.f, ms_total = 0.f;
   if (!cur.done && itn > 0) {
     const bool graph = ctx->opts.use_graph != 0;
     if (graph && (rc = ensure_graph(ctx))) return rc;
@@ -721,6 +756,7 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaEventSynchronize(ctx->ev1));
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    CK(cudaEventElapsedTime(&ms_total, ctx->ev_start, ctx->ev1));
   }
   if (ctx->want_se && done_itn > 0)
     k_finish_se<<<ctx->gvx, kThreads, 0, ctx->stream>>>(ctx->se, ctx->n, ctx->st, ctx->m_k + ctx->m_d);
@@ -750,6 +786,7 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   r.dxmax = cur.dxmax;
   r.maxdx = cur.maxdx;
   r.seconds = ms * 1e-3;
+  r.seconds_total = ms_total * 1e-3;
   if (res) *res = r;
   if (hist) memcpy(hist, hh.data(), sizeof(plsqr_iter) * (itn + 1));
   if (ctx->opts.verbose) print_iterations(hh.data(), r.itn, r.seconds);

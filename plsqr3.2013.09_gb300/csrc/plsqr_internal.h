@@ -38,7 +38,7 @@ struct MixedState;  // mixed.cu
 struct plsqr_ctx {
   plsqr_opts opts;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_start = nullptr;
   int32_t m_k = 0, m_d = 0, n = 0;
   int64_t nnz_k = 0, nnz_d = 0;
   int sm_count = 0, blocks_per_sm = 0, unroll = 2;
@@ -62,16 +62,25 @@ struct plsqr_ctx {
   char last_error[512] = {0};
   MixedState *mixed = nullptr;
   // slab layout of the kernel matrix (default FP64 product path)
-  bool use_slabs = false;  // FP64 products on slabs (opt-in)
+  bool use_slabs = false;  // FP64 A^T y on slabs
+  bool use_slabs_rows = false;  // FP64 A x on slabs
   bool slab_ok = false;    // dimensions fit the slab layout
+  int slab_group = 8;      // lanes per segment, FP64 slab products
+  int slab_group_f = 16;   // lanes per segment, FP32 slab products
   DevSlab<double> s_rows, s_cols;  // K by row (gathers v), K by column (gathers u_k)
   int gc1k = 1, gc1d = 1, gc2 = 1;  // grids of the combine kernels
 };
 
 // slab.cu
 template <typename T>
-int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevSlab<T> *out);
+int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, int blocks,
+               DevSlab<T> *out);
 int slab_plan(plsqr_ctx *ctx);
+// plsqr_gpu.cu: slab product launch and its shared-memory attribute
+template <typename T>
+void slab_spmv(const DevSlab<T> &S, int group, const T *x, cudaStream_t s);
+template <typename T>
+int slab_set_smem(size_t smem);
 // plsqr_gpu.cu: partial-sum counts of the current product path
 int ctx_pu_k(const plsqr_ctx *ctx);
 int ctx_pu_d(const plsqr_ctx *ctx);

@@ -27,7 +27,8 @@ constexpr int kMaxSlabs = 64;  // k_slab_count / k_slab_fill keep one counter pe
 }
 
 template <typename T>
-int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevSlab<T> *out) {
+int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, int blocks,
+               DevSlab<T> *out) {
   const int n_lines = L.n_lines;
   const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
   if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
@@ -66,8 +67,9 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, D
                                              out->idx, out->val);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
-  // blocks per slab: about two waves of one resident block per SM in total
-  int bps = std::max(1, (2 * ctx->sm_count + n_slabs - 1) / n_slabs);
+  // blocks per slab: `blocks` in total (several waves of small, nonzero-
+  // balanced line ranges; measured better than one wave of large ones)
+  int bps = std::max(1, (blocks + n_slabs - 1) / n_slabs);
   if (const char *e = getenv("PLSQR_SLAB_BLOCKS"))
     if (atoi(e) > 0) bps = std::max(1, atoi(e) / n_slabs);
   out->bps = bps;
@@ -91,35 +93,43 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, D
   return PLSQR_OK;
 }
 
-template int build_slab<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t, DevSlab<double> *);
-template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, DevSlab<float> *);
+template int build_slab<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t, int,
+                                DevSlab<double> *);
+template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, int,
+                               DevSlab<float> *);
 
-// Plan the slab path: slab_ok when every dimension fits kMaxSlabs slabs of
-// 49,152 FP32 values (the mixed solver's inner products always use slabs
-// then).  The FP64 products use the per-line kernels unless PLSQR_SLABS=1
-// asks for FP64 slabs: measured on the 96x96x32 problem, splitting each line
-// into slab segments adds one warp reduction per segment on the FP64 pipe,
-// which costs more than the shared-memory gathers save.
+// Plan the slab paths.  slab_ok: every dimension fits kMaxSlabs slabs of
+// 24,576 FP32 values, so the mixed solver's inner products use FP32 slabs.
+// FP64: A^T y uses slabs of 24,576 values (its gathers of u_k scatter over
+// L2, and shared memory serves them faster); A x keeps the per-line kernel
+// (its gathers of v hit nearby columns and already run near the HBM
+// roofline, while slab segments would add FP64 reductions).  PLSQR_SLABS
+// overrides: 0 none, 1 both orientations, 2 A^T y only (default).
 int slab_plan(plsqr_ctx *ctx) {
-  ctx->use_slabs = false;
-  const int fslab = 49152;
+  ctx->use_slabs = ctx->use_slabs_rows = false;
+  const int fslab = 24576;
   ctx->slab_ok = ctx->nnz_k > 0 && (ctx->n + fslab - 1) / fslab <= kMaxSlabs &&
                  (ctx->m_k + fslab - 1) / fslab <= kMaxSlabs;
   const int sm = ctx->sm_count, half = kMaxParts / 2;
   ctx->gc1k = std::max(1, std::min({sm * 2, (ctx->m_k + 255) / 256, half}));
   ctx->gc1d = std::max(1, std::min({sm * 2, (ctx->m_d + 255) / 256, half}));
   ctx->gc2 = std::max(1, std::min({sm * 4, (ctx->n + 255) / 256, kMaxParts}));
-  const char *e = getenv("PLSQR_SLABS");
-  if (!e || atoi(e) != 1) return PLSQR_OK;
+  int mode = 2;
+  if (const char *e = getenv("PLSQR_SLABS")) mode = atoi(e);
   int slab = 24576;  // 192 KB of FP64 per block
   if (const char *s = getenv("PLSQR_SLAB_SIZE"))
     if (atoi(s) >= 1024 && atoi(s) <= 28672) slab = atoi(s);
-  const int ns_r = (ctx->n + slab - 1) / slab, ns_c = (ctx->m_k + slab - 1) / slab;
-  if (ns_r > kMaxSlabs || ns_c > kMaxSlabs || ctx->nnz_k == 0) return PLSQR_OK;
+  const bool rows_fit = (ctx->n + slab - 1) / slab <= kMaxSlabs;
+  const bool cols_fit = (ctx->m_k + slab - 1) / slab <= kMaxSlabs;
+  if (ctx->nnz_k == 0 || mode <= 0) return PLSQR_OK;
   int rc;
-  if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, &ctx->s_rows)) ||
-      (rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, &ctx->s_cols)))
-    return rc;
-  ctx->use_slabs = true;
+  if (mode == 1 && rows_fit) {
+    if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &ctx->s_rows))) return rc;
+    ctx->use_slabs_rows = true;
+  }
+  if ((mode == 1 || mode == 2) && cols_fit) {
+    if ((rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &ctx->s_cols))) return rc;
+    ctx->use_slabs = true;
+  }
   return PLSQR_OK;
 }

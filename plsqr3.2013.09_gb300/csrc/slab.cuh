@@ -99,11 +99,15 @@ __device__ __forceinline__ void load8(const float *v, int64_t g, float (&o)[8]) 
 
 // partial[s * n_lines + l] = sum over segment (s, l) of val * x_slab[idx].
 // Blocks are slab-major: slab s = blockIdx.x / bps, range r = blockIdx.x % bps;
-// lpart[s * (bps + 1) + r] .. [.. + 1] is the range's first and end line.
-template <typename T, int kThreads>
+// lpart[s * (bps + 1) + r] .. [.. + 1] is the range's first and end line.  A
+// group of kGroup lanes streams one segment (each lane one 16-byte group of 8
+// indices per step) and reduces it in log2(kGroup) shuffles, so that a short
+// segment does not pay a full 5-step warp reduction on the FP64 pipe.
+template <typename T, int kThreads, int kGroup>
 __global__ void __launch_bounds__(kThreads)
     k_slab_spmv(SlabCsr<T> A, const int32_t *__restrict__ lpart, int bps, const T *__restrict__ x,
                 T *__restrict__ partial) {
+  static_assert(kGroup == 4 || kGroup == 8 || kGroup == 16 || kGroup == 32, "4 to 32 lanes");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *xs = reinterpret_cast<T *>(smem_raw);
   const int s = blockIdx.x / bps, r = blockIdx.x - s * bps;
@@ -111,36 +115,48 @@ __global__ void __launch_bounds__(kThreads)
   const int len = (int)min((int64_t)A.slab, (int64_t)A.n_idx - base);
   for (int i = threadIdx.x; i < len; i += kThreads) xs[i] = x[base + i];
   __syncthreads();
-  const int lane = threadIdx.x & 31;
+  const int sub = threadIdx.x & (kGroup - 1);        // lane within the group
+  const int grp = threadIdx.x / kGroup;              // group within the block
+  constexpr int kGroups = kThreads / kGroup;
   const int64_t *ptr = A.ptr + (int64_t)s * (A.n_lines + 1);
   const int l1 = lpart[s * (bps + 1) + r + 1];
   const uint4 *idx8 = reinterpret_cast<const uint4 *>(A.idx);
-  for (int l = lpart[s * (bps + 1) + r] + (threadIdx.x >> 5); l < l1; l += kThreads / 32) {
-    const int64_t g0 = ptr[l] >> 3, g1 = ptr[l + 1] >> 3;  // groups of 8 entries
+  // every group runs the same number of loop trips so the shuffles below
+  // always see their whole group
+  const int l0 = lpart[s * (bps + 1) + r];
+  for (int lb = l0; lb < l1; lb += kGroups) {
+    const int l = lb + grp;
     T acc0 = 0, acc1 = 0;
-    for (int64_t g = g0 + lane; g < g1; g += 32) {
-      const uint4 q = __ldg(idx8 + g);
-      T v[8];
-      load8(A.val, g, v);
-      acc0 = fmaT(v[0], xs[q.x & 0xffff], acc0);
-      acc1 = fmaT(v[1], xs[q.x >> 16], acc1);
-      acc0 = fmaT(v[2], xs[q.y & 0xffff], acc0);
-      acc1 = fmaT(v[3], xs[q.y >> 16], acc1);
-      acc0 = fmaT(v[4], xs[q.z & 0xffff], acc0);
-      acc1 = fmaT(v[5], xs[q.z >> 16], acc1);
-      acc0 = fmaT(v[6], xs[q.w & 0xffff], acc0);
-      acc1 = fmaT(v[7], xs[q.w >> 16], acc1);
+    if (l < l1) {
+      const int64_t g0 = ptr[l] >> 3, g1 = ptr[l + 1] >> 3;  // groups of 8 entries
+      for (int64_t g = g0 + sub; g < g1; g += kGroup) {
+        const uint4 q = __ldg(idx8 + g);
+        T v[8];
+        load8(A.val, g, v);
+        acc0 = fmaT(v[0], xs[q.x & 0xffff], acc0);
+        acc1 = fmaT(v[1], xs[q.x >> 16], acc1);
+        acc0 = fmaT(v[2], xs[q.y & 0xffff], acc0);
+        acc1 = fmaT(v[3], xs[q.y >> 16], acc1);
+        acc0 = fmaT(v[4], xs[q.z & 0xffff], acc0);
+        acc1 = fmaT(v[5], xs[q.z >> 16], acc1);
+        acc0 = fmaT(v[6], xs[q.w & 0xffff], acc0);
+        acc1 = fmaT(v[7], xs[q.w >> 16], acc1);
+      }
     }
-    const T t = warp_sum(acc0 + acc1);
-    if (lane == 0) partial[(int64_t)s * A.n_lines + l] = t;
+    T t = acc0 + acc1;
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (sub == 0 && l < l1) partial[(int64_t)s * A.n_lines + l] = t;
   }
 }
 
 // u_k[r] = scale*u_k[r] + sum_s partial[s][r] (blocks [0, gk)); u_d[r] =
 // scale*u_d[r] + (D v)[r] (blocks [gk, grid)); per-block sums of squares.
-template <typename T, int kThreads>
+// P: type of the slab partials, T: type of the vectors (the mixed solver
+// combines FP32 partials into FP64 vectors).
+template <typename P, typename T, int kThreads>
 __global__ void __launch_bounds__(kThreads)
-    k_combine_rows(const T *__restrict__ partial, int n_slabs, int m_k, Csr D,
+    k_combine_rows(const P *__restrict__ partial, int n_slabs, int m_k, Csr D,
                    const T *__restrict__ v, T *__restrict__ u, int gk, int mode,
                    const DevState *__restrict__ st, double *__restrict__ parts) {
   __shared__ double smem[kThreads / 32];
@@ -150,7 +166,7 @@ __global__ void __launch_bounds__(kThreads)
   if ((int)blockIdx.x < gk) {
     for (int r = blockIdx.x * kThreads + threadIdx.x; r < m_k; r += gk * kThreads) {
       T t = 0;
-      for (int q = 0; q < n_slabs; ++q) t += partial[(int64_t)q * m_k + r];
+      for (int q = 0; q < n_slabs; ++q) t += (T)partial[(int64_t)q * m_k + r];
       const T y = scaled_add(s, u[r], t);
       u[r] = y;
       sq = fma((double)y, (double)y, sq);
@@ -181,9 +197,9 @@ __device__ __forceinline__ float damp_col(const Csr &DC, const float *__restrict
 
 // v[c] = scale*v[c] + (sum_s partial[s][c] + (D^T u_d)[c]); per-block sums
 // of squares.  LSQR mode: skipped when beta == 0 (source/lsqr.c:530).
-template <typename T, int kThreads>
+template <typename P, typename T, int kThreads>
 __global__ void __launch_bounds__(kThreads)
-    k_combine_cols(const T *__restrict__ partial, int n_slabs, int n, Csr DC,
+    k_combine_cols(const P *__restrict__ partial, int n_slabs, int n, Csr DC,
                    const T *__restrict__ u, int m_k, T *__restrict__ v, int mode,
                    const DevState *__restrict__ st, double *__restrict__ parts) {
   __shared__ double smem[kThreads / 32];
@@ -199,7 +215,7 @@ __global__ void __launch_bounds__(kThreads)
   double sq = 0.0;
   for (int c = blockIdx.x * kThreads + threadIdx.x; c < n; c += gridDim.x * kThreads) {
     T t = 0;
-    for (int q = 0; q < n_slabs; ++q) t += partial[(int64_t)q * n + c];
+    for (int q = 0; q < n_slabs; ++q) t += (T)partial[(int64_t)q * n + c];
     const T y = scaled_add(s, v[c], t + damp_col(DC, ud, c));  // x += (s_k + s_d)
     v[c] = y;
     sq = fma((double)y, (double)y, sq);

@@ -34,6 +34,10 @@ CONFIGS: dict[str, dict] = {
 # the 96x96x32 grid with a tenth of the rays (~1.3e8 kernel nonzeros, ~3 GB on
 # the device): large enough to stream from HBM, small enough to profile
 CONFIGS["grid96s"] = dict(CONFIGS["grid96"], n_rays=20000)
+# a 48x48x32 grid with 40,000 radius-6 rays (~1.8e8 nonzeros, ~4,500 per row
+# and ~2,500 per column, ~4.5 GB on the device): line lengths close to the
+# 96x96x32 problem's, for kernel profiles
+CONFIGS["grid48p"] = dict(CONFIGS["grid96"], nx=48, ny=48, n_rays=40000)
 
 # the reference's file names for a generated problem (data/LSQR_run/LSQR3.pbs:10)
 FILE_NAMES = dict(ker_f="matrix_bycol.mm2.bin", ker_i="matrix_bycol.mm2.info",
