@@ -6,7 +6,7 @@
 namespace plsqr {
 
 // Maximum number of per-block partial sums a reduction kernel may write.
-constexpr int kMaxParts = 8192;
+constexpr int kMaxParts = 16384;
 
 struct DevState {
   // lsqr() arguments (source/lsqr.h:32-62)

@@ -178,12 +178,14 @@ __device__ __forceinline__ float damp_row(const Csr &D, const float *__restrict_
 }
 
 // ---------------------------------------------------------------------------
-// M1: u_k[r] = s*u_k[r] + (K v)[r], u_d[r] = s*u_d[r] + (D v)[r]; per-block
-// partial sums of squares of the new u (in FP64): parts[0..gk) kernel rows,
-// parts[gk..gk+gd) damping rows.  Warp w of the kernel blocks owns rows
-// [kpart[w], kpart[w+1]), a contiguous range holding about the same number of
-// nonzeros as every other warp's.  T = double: the FP64 solver; T = float:
-// the inner sweeps of the mixed solver (values: the FP32 high half).
+// M1: u_k[r] = s*u_k[r] + (K v)[r], u_d[r] = s*u_d[r] + (D v)[r], with the
+// sums of squares of the new u (in FP64): one partial per warp of the kernel
+// blocks, parts[0 .. gk*kThreads/32), then one per damping block.  Warp w of
+// the kernel blocks owns rows [kpart[w], kpart[w+1]), a contiguous range
+// holding about the same number of nonzeros as every other warp's; writing a
+// partial per warp lets a warp that finishes early leave without waiting at
+// a block barrier.  T = double: the FP64 solver; T = float: the inner sweeps
+// of the mixed solver (values: the FP32 high half).
 template <typename T, int kThreads, int kUnroll>
 __global__ void __launch_bounds__(kThreads)
     k_aprod1(CsrT<T> K, Csr D, const int32_t *__restrict__ kpart, const T *__restrict__ v,
@@ -205,18 +207,18 @@ __global__ void __launch_bounds__(kThreads)
         sq = fma((double)y, (double)y, sq);
       }
     }
-  } else {
-    const int gd = gridDim.x - gk;
-    T *ud = u + K.n_lines;
-    for (int r = (blockIdx.x - gk) * kThreads + threadIdx.x; r < D.n_lines;
-         r += gd * kThreads) {
-      const T y = scaled_add(s, ud[r], damp_row(D, v, r));
-      ud[r] = y;
-      sq = fma((double)y, (double)y, sq);
-    }
+    if (lane == 0 && parts) parts[w] = sq;
+    return;
+  }
+  const int gd = gridDim.x - gk;
+  T *ud = u + K.n_lines;
+  for (int r = (blockIdx.x - gk) * kThreads + threadIdx.x; r < D.n_lines; r += gd * kThreads) {
+    const T y = scaled_add(s, ud[r], damp_row(D, v, r));
+    ud[r] = y;
+    sq = fma((double)y, (double)y, sq);
   }
   const double b = block_sum<kThreads>(sq, smem);
-  if (threadIdx.x == 0 && parts) parts[blockIdx.x] = b;
+  if (threadIdx.x == 0 && parts) parts[gk * (kThreads / 32) + (blockIdx.x - gk)] = b;
 }
 
 // ---------------------------------------------------------------------------

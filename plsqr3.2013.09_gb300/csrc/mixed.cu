@@ -82,8 +82,8 @@ int mixed_prepare(plsqr_ctx *ctx) {
     int slab = 24576;  // 96 KB of FP32 per block: two blocks per SM
     if (const char *e = getenv("PLSQR_SLAB_SIZE_F"))
       if (atoi(e) >= 1024 && atoi(e) <= 57344) slab = atoi(e);
-    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 8 * ctx->sm_count, &M->s_rows)) ||
-        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 8 * ctx->sm_count, &M->s_cols)))
+    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &M->s_rows)) ||
+        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &M->s_cols)))
       return rc;
     if ((rc = slab_set_smem<float>(std::max(M->s_rows.smem, M->s_cols.smem)))) return rc;
     M->slabs = true;
@@ -94,7 +94,7 @@ int mixed_prepare(plsqr_ctx *ctx) {
 }
 
 // partial-sum counts of the inner products (slab combine grids or per-line grids)
-static int pu_k(const plsqr_ctx *ctx) { return ctx->mixed->slabs ? ctx->gc1k : ctx->g1k; }
+static int pu_k(const plsqr_ctx *ctx) { return ctx->mixed->slabs ? ctx->gc1k : ctx->g1k * (kThreads / 32); }
 static int pu_d(const plsqr_ctx *ctx) { return ctx->mixed->slabs ? ctx->gc1d : ctx->g1d; }
 static int pv(const plsqr_ctx *ctx) { return ctx->mixed->slabs ? ctx->gc2 : ctx->g2; }
 

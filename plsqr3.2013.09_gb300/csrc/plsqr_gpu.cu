@@ -191,7 +191,7 @@ static void launch_m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
 // (mode 2) per-block sums of squares for the norm kernels.
 template <typename T>
 void slab_spmv(const DevSlab<T> &S, int group, const T *x, cudaStream_t s) {
-  const SlabCsr<T> A{S.ptr, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx};
+  const SlabCsr<T> A{S.ptr, S.order, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx};
   const int grid = S.n_slabs * S.bps;
   if (group == 4)
     k_slab_spmv<T, 1024, 4><<<grid, 1024, S.smem, s>>>(A, S.lpart, S.bps, x, S.partial);
@@ -256,7 +256,9 @@ static int slab_attrs(plsqr_ctx *ctx) {
 }
 
 // partial-sum counts the norm kernels read
-int ctx_pu_k(const plsqr_ctx *ctx) { return ctx->use_slabs_rows ? ctx->gc1k : ctx->g1k; }
+int ctx_pu_k(const plsqr_ctx *ctx) {
+  return ctx->use_slabs_rows ? ctx->gc1k : ctx->g1k * (kThreads / 32);  // k_aprod1: per warp
+}
 int ctx_pu_d(const plsqr_ctx *ctx) { return ctx->use_slabs_rows ? ctx->gc1d : ctx->g1d; }
 int ctx_pv(const plsqr_ctx *ctx) { return ctx->use_slabs ? ctx->gc2 : ctx->g2; }
 
@@ -295,10 +297,11 @@ static int plan_launch(plsqr_ctx *ctx, const std::vector<int64_t> &kc_ptr) {
   int occ1 = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_aprod1<double, kThreads, 2>, kThreads, 0));
   occ1 = std::max(1, std::min(occ1, ctx->blocks_per_sm));
-  // every reduction kernel writes one partial per block: at most kMaxParts
+  // every reduction kernel writes at most kMaxParts partials
   const int half = kMaxParts / 2;
-  // mode 1: one resident wave of warps over kernel rows, threads over damping rows
-  ctx->g1k = std::max(1, std::min({sm * occ1, (ctx->m_k + wpb - 1) / wpb, half}));
+  // mode 1: one resident wave of warps over kernel rows (one partial per
+  // warp), threads over damping rows (one partial per block)
+  ctx->g1k = std::max(1, std::min({sm * occ1, (ctx->m_k + wpb - 1) / wpb, half / wpb}));
   ctx->g1d = std::max(1, std::min({sm, (ctx->m_d + kThreads - 1) / kThreads, half}));
   // mode 2: many small blocks of neighbouring columns (several waves)
   int m2b = ctx->m2_blocks_per_sm;

@@ -28,6 +28,7 @@ struct DevSlab {
   int32_t n_lines = 0, n_slabs = 0, slab = 0, n_idx = 0;
   int64_t nnz_padded = 0;
   int32_t *lpart = nullptr;  // [n_slabs * (bps + 1)] line ranges of the blocks
+  int32_t *order = nullptr;  // [n_slabs * n_lines] visit order inside each range
   int bps = 0;               // blocks per slab
   T *partial = nullptr;      // [n_slabs * n_lines]
   size_t smem = 0;           // shared memory per block

@@ -86,8 +86,22 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, i
     }
     o[bps] = n_lines;
   }
-  if ((rc = dev_alloc(ctx, &out->lpart, lp.size()))) return rc;
+  // visit order inside every block range: longest segment first, ties by line
+  std::vector<int32_t> ord((size_t)n_slabs * n_lines);
+  for (int s = 0; s < n_slabs; ++s) {
+    const int64_t *seg = sp.data() + (size_t)s * (n_lines + 1);
+    int32_t *o = ord.data() + (size_t)s * n_lines;
+    for (int l = 0; l < n_lines; ++l) o[l] = l;
+    const int32_t *b = lp.data() + (size_t)s * (bps + 1);
+    for (int r = 0; r < bps; ++r)
+      std::stable_sort(o + b[r], o + b[r + 1], [&](int32_t a, int32_t c) {
+        return seg[a + 1] - seg[a] > seg[c + 1] - seg[c];
+      });
+  }
+  if ((rc = dev_alloc(ctx, &out->lpart, lp.size())) || (rc = dev_alloc(ctx, &out->order, ord.size())))
+    return rc;
   CK(cudaMemcpy(out->lpart, lp.data(), sizeof(int32_t) * lp.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(out->order, ord.data(), sizeof(int32_t) * ord.size(), cudaMemcpyHostToDevice));
   // the launching translation unit sets the kernel's shared-memory limit
   out->smem = sizeof(T) * (size_t)std::min(slab, n_idx);
   return PLSQR_OK;

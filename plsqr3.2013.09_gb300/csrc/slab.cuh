@@ -27,6 +27,7 @@ namespace plsqr {
 template <typename T>
 struct SlabCsr {
   const int64_t *ptr;   // [n_slabs * (n_lines + 1)]
+  const int32_t *order; // [n_slabs * n_lines] lines of each block range, longest segment first
   const uint16_t *idx;  // slab-local indices
   const T *val;
   int32_t n_lines;      // lines (rows for A x, columns for A^T y)
@@ -103,8 +104,10 @@ __device__ __forceinline__ void load8(const float *v, int64_t g, float (&o)[8]) 
 // group of kGroup lanes streams one segment (each lane one 16-byte group of 8
 // indices per step) and reduces it in log2(kGroup) shuffles, so that a short
 // segment does not pay a full 5-step warp reduction on the FP64 pipe.
+// FP32 slabs are 96 KB, so two blocks share an SM: the register budget must
+// allow it (32 registers per thread at 1024 threads).
 template <typename T, int kThreads, int kGroup>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     k_slab_spmv(SlabCsr<T> A, const int32_t *__restrict__ lpart, int bps, const T *__restrict__ x,
                 T *__restrict__ partial) {
   static_assert(kGroup == 4 || kGroup == 8 || kGroup == 16 || kGroup == 32, "4 to 32 lanes");
@@ -121,15 +124,43 @@ __global__ void __launch_bounds__(kThreads)
   const int64_t *ptr = A.ptr + (int64_t)s * (A.n_lines + 1);
   const int l1 = lpart[s * (bps + 1) + r + 1];
   const uint4 *idx8 = reinterpret_cast<const uint4 *>(A.idx);
-  // every group runs the same number of loop trips so the shuffles below
-  // always see their whole group
+  const int32_t *order = A.order + (int64_t)s * A.n_lines;
+  // The lines of the range are visited longest segment first, so the groups
+  // of a warp walk segments of about the same length.  Every group runs the
+  // same number of loop trips so the shuffles below see their whole group.
   const int l0 = lpart[s * (bps + 1) + r];
   for (int lb = l0; lb < l1; lb += kGroups) {
-    const int l = lb + grp;
+    const int k = lb + grp;
+    const int l = k < l1 ? order[k] : 0;
     T acc0 = 0, acc1 = 0;
-    if (l < l1) {
+    if (k < l1) {
       const int64_t g0 = ptr[l] >> 3, g1 = ptr[l + 1] >> 3;  // groups of 8 entries
-      for (int64_t g = g0 + sub; g < g1; g += kGroup) {
+      int64_t g = g0 + sub;
+      // FP64: two steps in flight; FP32 keeps one to stay within 32 registers
+      constexpr int kSteps = sizeof(T) == 8 ? 2 : 1;
+      for (; kSteps == 2 && g + kGroup < g1; g += 2 * kGroup) {
+        const uint4 q = __ldg(idx8 + g), p = __ldg(idx8 + g + kGroup);
+        T v[8], w[8];
+        load8(A.val, g, v);
+        load8(A.val, g + kGroup, w);
+        acc0 = fmaT(v[0], xs[q.x & 0xffff], acc0);
+        acc1 = fmaT(v[1], xs[q.x >> 16], acc1);
+        acc0 = fmaT(v[2], xs[q.y & 0xffff], acc0);
+        acc1 = fmaT(v[3], xs[q.y >> 16], acc1);
+        acc0 = fmaT(v[4], xs[q.z & 0xffff], acc0);
+        acc1 = fmaT(v[5], xs[q.z >> 16], acc1);
+        acc0 = fmaT(v[6], xs[q.w & 0xffff], acc0);
+        acc1 = fmaT(v[7], xs[q.w >> 16], acc1);
+        acc0 = fmaT(w[0], xs[p.x & 0xffff], acc0);
+        acc1 = fmaT(w[1], xs[p.x >> 16], acc1);
+        acc0 = fmaT(w[2], xs[p.y & 0xffff], acc0);
+        acc1 = fmaT(w[3], xs[p.y >> 16], acc1);
+        acc0 = fmaT(w[4], xs[p.z & 0xffff], acc0);
+        acc1 = fmaT(w[5], xs[p.z >> 16], acc1);
+        acc0 = fmaT(w[6], xs[p.w & 0xffff], acc0);
+        acc1 = fmaT(w[7], xs[p.w >> 16], acc1);
+      }
+      for (; g < g1; g += kGroup) {
         const uint4 q = __ldg(idx8 + g);
         T v[8];
         load8(A.val, g, v);
@@ -146,7 +177,7 @@ __global__ void __launch_bounds__(kThreads)
     T t = acc0 + acc1;
 #pragma unroll
     for (int o = kGroup / 2; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (sub == 0 && l < l1) partial[(int64_t)s * A.n_lines + l] = t;
+    if (sub == 0 && k < l1) partial[(int64_t)s * A.n_lines + l] = t;
   }
 }
 
