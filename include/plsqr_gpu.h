@@ -228,6 +228,108 @@ int plsqr_aprod1_nrm2_noalloc(int32_t n_rows, const int64_t *row_ptr,
                               const double *x, double *y, double *nrm2,
                               void *stream);
 
+/* ---- several right-hand sides on one operator ---------------------------
+ * No counterpart in the reference, whose lsqr() solves one right-hand side
+ * per run (source/lsqr.c:195-917).  These entries advance k <= 32 LSQR solves
+ * in lock step on the context's matrix, one k-wide product per matrix read:
+ * right-hand side j solves min || [K; lambda_j D] x_j - [b_j; 0] || (the
+ * damping rows weighted by lambda_j).  The form is the refinement solver of
+ * PLSQR_PREC_MIXED: `sweeps` FP64 residuals b - A x over the FP64 kernel
+ * values, each followed by `inner` LSQR iterations whose kernel products use
+ * the FP32 high half of the value split while vectors, norms and the scalar
+ * recurrences stay FP64. */
+#define PLSQR_BATCH_MAX 32
+typedef struct {
+  int32_t k;             /* right-hand sides, 1 .. PLSQR_BATCH_MAX            */
+  int32_t sweeps, inner; /* refinement sweeps, LSQR iterations per sweep      */
+  int32_t variant_rows;  /* product variant of A x (plsqr_batch_variant), or
+                            -1 = pick by timing (cached per operator shape)  */
+  int32_t variant_cols;  /* the same for A^T y                                */
+  int32_t pad;
+  double damp, atol, btol, conlim; /* lsqr() arguments of every solve         */
+  const double *b_k;     /* [k][m_k]: right-hand side j at b_k + j*m_k        */
+  const double *lambda;  /* [k] damping-row weights; NULL = all 1             */
+  const double *x_ref;   /* [k][n] solutions to measure the error against
+                            (history field err), or NULL                      */
+} plsqr_batch_args;
+void plsqr_default_batch_args(plsqr_batch_args *a);
+
+/* Product variants: kVW-wide gathers (4 = float4, 2 = float2), kLPR lanes per
+ * line, kU nonzeros in flight per lane.  Returns PLSQR_ERR_ARG past the last. */
+int plsqr_batch_variant(int32_t index, int32_t *vw, int32_t *lanes_per_line,
+                        int32_t *unroll);
+
+typedef struct {
+  int32_t k, kp;                    /* right-hand sides, padded block width   */
+  int32_t variant_rows, variant_cols; /* variants in use                      */
+  int32_t tuned;                    /* 1: timed by the last call, 0: cached   */
+  int32_t pad;
+  double ms_rows, ms_cols;          /* their times per product when timed     */
+} plsqr_batch_info;
+
+/* Solve; x: [k][n] (or NULL), hist: [k][sweeps*inner + 1] (or NULL; entry 0
+ * is the start of the first sweep), res: [k] (or NULL). */
+int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, double *x,
+                     plsqr_iter *hist, plsqr_result *res, plsqr_batch_info *info);
+/* Time one k-wide product (mode 1: A x, mode 2: A^T y) of a variant (-1 =
+ * the tuned one), averaged over reps launches, after one untimed launch. */
+int plsqr_batch_bench_aprod(plsqr_ctx *ctx, int32_t k, int mode, int32_t variant,
+                            int reps, double *ms_per_launch);
+
+/* ---- independent problems in one persistent launch ----------------------
+ * No counterpart in the reference, which solves one problem per run.  Each
+ * problem is a complete lsqr() of lsqr_iteration iterations in FP64 (the
+ * reference's arithmetic, source/lsqr.c:195-917), on its own operator
+ * [K; D] and right-hand side.  One cooperative kernel launch runs all of them:
+ * a host planner gives every problem a group of thread blocks (in proportion
+ * to its work, several small problems queued on one group when blocks run
+ * out), and each group works through its queue, its blocks meeting at
+ * barriers in device memory.  Every barrier wait is bounded (wait_ns): past
+ * the limit the launch ends and the solve returns PLSQR_ERR_TIMEOUT. */
+typedef struct {
+  plsqr_sparse k_csc, d_csr, d_csc; /* as for plsqr_ctx_create              */
+  const double *b_k;                /* [k_csc.num_row]                      */
+  int32_t lsqr_iteration;           /* iterations run (as plsqr_lsqr_args)  */
+  int32_t itnlim;
+  double damp, atol, btol, conlim;
+} plsqr_problem;
+void plsqr_default_problem(plsqr_problem *p); /* call_lsqr's constants */
+
+typedef struct plsqr_multi plsqr_multi;
+typedef struct {
+  int32_t count;         /* problems                                        */
+  int32_t blocks;        /* thread blocks of the persistent launch          */
+  int32_t groups;        /* block groups (each runs a queue of problems)    */
+  int32_t blocks_per_sm; /* resident blocks per SM of the launch            */
+  int64_t device_bytes;  /* device memory held                              */
+  int64_t wait_ns;       /* limit of one barrier wait                       */
+  double seconds;        /* device time of the last solve                   */
+} plsqr_multi_info;
+
+/* Uploads the problems (copied; the caller's arrays may be freed after). */
+int plsqr_multi_create(const plsqr_problem *probs, int32_t count,
+                       const plsqr_opts *opts, plsqr_multi **out);
+void plsqr_multi_destroy(plsqr_multi *mp);
+const char *plsqr_multi_last_error(const plsqr_multi *mp);
+int plsqr_multi_info_get(const plsqr_multi *mp, plsqr_multi_info *info);
+/* The plan: group[p] of every problem and the blocks of every group
+ * (arrays of count entries; group_blocks entries past info.groups are 0). */
+int plsqr_multi_plan(const plsqr_multi *mp, int32_t *group, int32_t *group_blocks);
+/* Set the barrier wait limit (nanoseconds, >= 1000); default one second. */
+int plsqr_multi_set_wait(plsqr_multi *mp, int64_t wait_ns);
+/* Solve all problems.  x: the solutions one after another (sum of n_p
+ * values) or NULL; hist: lsqr_iteration_p + 1 records per problem, one after
+ * another, or NULL; res: [count] or NULL. */
+int plsqr_multi_solve(plsqr_multi *mp, double *x, plsqr_iter *hist, plsqr_result *res);
+/* Runs one bounded wait on a flag that nothing sets, on the device, with the
+ * given limit: returns PLSQR_ERR_TIMEOUT and leaves the context usable. */
+int plsqr_multi_check_wait(plsqr_multi *mp, int64_t wait_ns);
+
+/* Weight the context's damping rows: D becomes lambda * D (both copies, from
+ * the values the context was created with).  For one-right-hand-side solves
+ * of the weighted problems above. */
+int plsqr_set_damping_weight(plsqr_ctx *ctx, double lambda);
+
 /* ---- files, host side (no GPU needed) ----------------------------------- */
 /* read_kernel_col_info (plsqr3.c:1379-1409): nnz[n], start[n] (0-based,
  * -1 where the file has 0) and the total. */
@@ -292,6 +394,11 @@ int plsqr_synth_xtrue(const plsqr_synth_params *p, double *x);
 int plsqr_synth_rhs(const plsqr_synth_params *p, const int64_t *row_ptr,
                     const int32_t *col_idx, const double *val,
                     const double *xtrue, double *b);
+/* b = kx + noise_frac * rms(kx) * N(0,1) with the normals of `noise_seed`
+ * (plsqr_synth_rhs adds those of p->seed to K x_true): the same measurements
+ * with another noise realisation. */
+int plsqr_synth_noisy(const plsqr_synth_params *p, uint64_t noise_seed, int64_t m,
+                      const double *kx, double *b);
 /* CSR <-> CSC transpose; output lines keep ascending input-line order. */
 int plsqr_transpose(int64_t n_lines, int64_t n_out, const int64_t *ptr,
                     const int32_t *idx, const double *val, int64_t *tptr,

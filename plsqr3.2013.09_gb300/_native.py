@@ -70,6 +70,17 @@ class SynthParams(C.Structure):
                 ("damp_identity", f64), ("damp_lap", f64), ("seed", u64)]
 
 
+class BatchArgs(C.Structure):
+    _fields_ = [("k", i32), ("sweeps", i32), ("inner", i32), ("variant_rows", i32),
+                ("variant_cols", i32), ("pad", i32), ("damp", f64), ("atol", f64),
+                ("btol", f64), ("conlim", f64), ("b_k", vp), ("lambda_", vp), ("x_ref", vp)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("k", i32), ("kp", i32), ("variant_rows", i32), ("variant_cols", i32),
+                ("tuned", i32), ("pad", i32), ("ms_rows", f64), ("ms_cols", f64)]
+
+
 ITER_DTYPE = np.dtype([(k, "<f8") for k in ("alpha", "beta", "rnorm", "arnorm", "test1", "test2",
                                              "anorm", "acond", "xnorm", "x0", "err")]
                       + [("istop", "<i4"), ("pad", "<i4")])
@@ -101,6 +112,11 @@ SIGNATURES = {
     "plsqr_bench_aprod": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(f64)]),
     "plsqr_bench_iteration": (C.c_int, [vp, C.c_int, C.POINTER(f64)]),
     "plsqr_aprod1_nrm2_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "plsqr_default_batch_args": (None, [C.POINTER(BatchArgs)]),
+    "plsqr_batch_variant": (C.c_int, [i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),
+    "plsqr_batch_lsqr": (C.c_int, [vp, C.POINTER(BatchArgs), vp, vp, vp, C.POINTER(BatchInfo)]),
+    "plsqr_batch_bench_aprod": (C.c_int, [vp, i32, C.c_int, i32, C.c_int, C.POINTER(f64)]),
+    "plsqr_set_damping_weight": (C.c_int, [vp, f64]),
     "plsqr_io_read_kernel_info": (C.c_int, [C.c_char_p, i32, vp, vp, C.POINTER(i64)]),
     "plsqr_io_read_kernel": (C.c_int, [C.c_char_p, C.c_char_p, i32, i32, vp, vp, vp]),
     "plsqr_io_read_int32_counts": (C.c_int, [C.c_char_p, i64, vp, C.POINTER(i64)]),
@@ -119,6 +135,7 @@ SIGNATURES = {
     "plsqr_synth_damping_fill": (C.c_int, [C.POINTER(SynthParams), vp, vp, vp]),
     "plsqr_synth_xtrue": (C.c_int, [C.POINTER(SynthParams), vp]),
     "plsqr_synth_rhs": (C.c_int, [C.POINTER(SynthParams), vp, vp, vp, vp, vp]),
+    "plsqr_synth_noisy": (C.c_int, [C.POINTER(SynthParams), u64, i64, vp, vp]),
     "plsqr_transpose": (C.c_int, [i64, i64, vp, vp, vp, vp, vp, vp]),
 }
 
@@ -165,3 +182,12 @@ def device_count() -> int:
     n = i32(0)
     check(lib().plsqr_device_count(C.byref(n)), "plsqr_device_count")
     return int(n.value)
+
+
+def batch_variant(index: int) -> tuple[int, int, int]:
+    """(gather width, lanes per line, nonzeros in flight) of a batched
+    product variant; PlsqrError past the last one."""
+    vw, lpr, u = i32(0), i32(0), i32(0)
+    check(lib().plsqr_batch_variant(index, C.byref(vw), C.byref(lpr), C.byref(u)),
+          "plsqr_batch_variant")
+    return vw.value, lpr.value, u.value

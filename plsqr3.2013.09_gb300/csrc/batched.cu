@@ -1,0 +1,578 @@
+// Several right-hand sides on one operator: k LSQR solves in lock step
+// (kernels_batched.cuh), with the refinement form of the mixed solver
+//
+//   X = 0
+//   repeat `sweeps` times:
+//     R  = [B; 0] - A_j X_j                 FP64 kernel values, per column j
+//     DX = LSQR(A_hi, R), `inner` iterations, one k-wide product per matrix read
+//     X += DX
+//
+// where A_j = [K; lambda_j D].  The inner iteration is four kernels captured
+// as one CUDA graph: A x, scaling of u, A^T y, scaling of v with the x/w update
+// and the scalar tail.  The product variant (gather width, lanes per line,
+// nonzeros in flight) of each direction is picked by timing the candidates on
+// the operator and cached per (line-length histogram, block width).
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels_batched.cuh"
+#include "kernels_f32.cuh"
+#include "plsqr_internal.h"
+
+using namespace plsqr;
+
+#define CK(call)                                                                 \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess) {                                                     \
+      ctx_set_error(ctx, "%s:%d %s: %s", __FILE__, __LINE__, #call,              \
+                    cudaGetErrorString(e_));                                     \
+      return PLSQR_ERR_CUDA;                                                     \
+    }                                                                            \
+  } while (0)
+
+struct BatchState;
+
+namespace {
+
+// ---- product variants ------------------------------------------------------
+using LaunchFn = void (*)(plsqr_ctx *, const BatchState &, int, cudaStream_t);
+
+struct Variant {
+  int vw, lpr, u;
+  LaunchFn rows, cols;
+};
+
+}  // namespace
+
+struct BatchState {
+  int kp = 0;  // block width the vectors are sized for
+  int kw = 4;  // block width of the current solve (a power of two <= kp)
+  float *k_hi = nullptr, *kc_hi = nullptr;
+  bool own_hi = false;
+  double *U = nullptr, *V = nullptr, *W = nullptr, *X = nullptr, *DX = nullptr;
+  double *B = nullptr, *XR = nullptr, *LAM = nullptr, *stage = nullptr;
+  float *Uf = nullptr, *Vf = nullptr;
+  DevState *st = nullptr;
+  BatchCoef *cf = nullptr;
+  double *parts = nullptr, *parts_dk = nullptr, *parts_err = nullptr;
+  int32_t *wrows = nullptr, *wcols = nullptr;
+  int gk = 1, gd = 1, gc = 1, gres = 1, gvec = 1;
+  int k = 0;  // right-hand sides of the current solve
+  bool has_ref = false;
+  int var_rows = -1, var_cols = -1;
+  double ms_rows = 0.0, ms_cols = 0.0;
+  int tuned = 0;
+  std::string shape;  // line-length histogram signature of the operator
+  plsqr_iter *hist = nullptr;
+  int64_t hist_cap = 0;
+  int hist_stride = 1;
+  cudaGraphExec_t graph = nullptr;
+  std::string graph_key;
+};
+
+namespace {
+
+template <int VW, int LPR, int U>
+void launch_rows(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  k_bprod_rows<VW, LPR, U><<<B.gk + B.gd, kBatchThreads, 0, s>>>(
+      CsrT<float>{ctx->K.ptr, ctx->K.idx, B.k_hi, ctx->K.n_lines}, ctx->D.csr(), B.wrows, B.gk,
+      B.kw, B.k, B.Vf, B.V, B.U, B.LAM, mode, B.st, B.cf, B.parts);
+}
+template <int VW, int LPR, int U>
+void launch_cols(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  k_bprod_cols<VW, LPR, U><<<B.gc, kBatchThreads, 0, s>>>(
+      CsrT<float>{ctx->KC.ptr, ctx->KC.idx, B.kc_hi, ctx->KC.n_lines}, ctx->DC.csr(), B.wcols,
+      B.kw, B.k, B.Uf, B.U, ctx->m_k, B.V, B.LAM, mode, B.st, B.cf, B.parts);
+}
+
+#define VARIANT(vw, lpr, u) \
+  Variant { vw, lpr, u, launch_rows<vw, lpr, u>, launch_cols<vw, lpr, u> }
+const Variant kVariants[] = {
+    VARIANT(4, 8, 1),  VARIANT(4, 8, 2),  VARIANT(4, 16, 1), VARIANT(4, 16, 2),
+    VARIANT(4, 32, 1), VARIANT(4, 32, 2), VARIANT(2, 16, 1), VARIANT(2, 16, 2),
+    VARIANT(2, 32, 1), VARIANT(2, 32, 2), VARIANT(2, 8, 1),  VARIANT(2, 8, 2),
+};
+#undef VARIANT
+constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+
+bool variant_ok(int v, int kp) {
+  if (v < 0 || v >= kNumVariants) return false;
+  const Variant &V = kVariants[v];
+  return kp % V.vw == 0 && kp / V.vw <= V.lpr;
+}
+
+int width_for(int k) {
+  int kp = 4;
+  while (kp < k) kp <<= 1;
+  return kp;
+}
+
+// Line-length histogram of an operator: per power-of-two length class, the
+// share of nonzeros in sixteenths.
+std::string length_signature(const std::vector<int64_t> &ptr) {
+  const int64_t n = (int64_t)ptr.size() - 1, nnz = ptr.back();
+  int64_t cls[40] = {0};
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t len = ptr[(size_t)i + 1] - ptr[(size_t)i];
+    int c = 0;
+    while ((int64_t(1) << c) < len && c < 39) ++c;
+    cls[c] += len;
+  }
+  std::string s;
+  for (int c = 0; c < 40; ++c) {
+    const int q = nnz > 0 ? (int)((cls[c] * 16 + nnz / 2) / nnz) : 0;
+    if (q > 0) s += std::to_string(c) + ":" + std::to_string(q) + ",";
+  }
+  return s;
+}
+
+// (signature | kp) -> (rows variant, cols variant), process-wide
+std::mutex g_tune_mu;
+std::map<std::string, std::pair<int, int>> g_tune_cache;
+
+void nnz_partition(const std::vector<int64_t> &pre, int parts, std::vector<int32_t> &out) {
+  const int32_t n = (int32_t)pre.size() - 1;
+  out.assign((size_t)parts + 1, 0);
+  const int64_t nnz = pre.back();
+  for (int w = 1; w < parts; ++w) {
+    const int64_t target = (int64_t)((long double)nnz * w / parts);
+    int32_t r = (int32_t)(std::lower_bound(pre.begin(), pre.end(), target) - pre.begin());
+    out[(size_t)w] = std::max(std::min(r, n), out[(size_t)w - 1]);
+  }
+  out[(size_t)parts] = n;
+}
+
+}  // namespace
+
+void batch_free(plsqr_ctx *ctx) {
+  if (!ctx || !ctx->batch) return;
+  if (ctx->batch->graph) cudaGraphExecDestroy(ctx->batch->graph);
+  delete ctx->batch;  // device buffers are in ctx->allocs
+  ctx->batch = nullptr;
+}
+
+static void free_vectors(plsqr_ctx *ctx, BatchState *B) {
+  for (void *p : {(void *)B->U, (void *)B->V, (void *)B->W, (void *)B->X, (void *)B->DX,
+                  (void *)B->B, (void *)B->XR, (void *)B->stage, (void *)B->Uf, (void *)B->Vf})
+    dev_free(ctx, p);
+  B->U = B->V = B->W = B->X = B->DX = B->B = B->XR = B->stage = nullptr;
+  B->Uf = B->Vf = nullptr;
+  B->kp = 0;
+}
+
+// Device buffers for blocks of width kp, the FP32 kernel values and the
+// per-warp line ranges of the products.
+static int batch_setup(plsqr_ctx *ctx);
+
+static int batch_prepare(plsqr_ctx *ctx, int kp) {
+  int rc;
+  if (!ctx->batch) {
+    ctx->batch = new BatchState();
+    if ((rc = batch_setup(ctx))) {
+      batch_free(ctx);  // its device buffers stay in ctx->allocs until destroy
+      return rc;
+    }
+  }
+  BatchState *B = ctx->batch;
+  if (B->kp >= kp) return PLSQR_OK;
+  if (B->graph) cudaGraphExecDestroy(B->graph);
+  B->graph = nullptr;
+  B->graph_key.clear();
+  free_vectors(ctx, B);
+  const size_t m = (size_t)ctx->m_k + ctx->m_d, n = (size_t)ctx->n, mk = (size_t)ctx->m_k;
+  const size_t big = std::max(std::max(m, n), (size_t)1);
+  if ((rc = dev_alloc(ctx, &B->U, m * kp)) || (rc = dev_alloc(ctx, &B->V, n * kp)) ||
+      (rc = dev_alloc(ctx, &B->W, n * kp)) || (rc = dev_alloc(ctx, &B->X, n * kp)) ||
+      (rc = dev_alloc(ctx, &B->DX, n * kp)) || (rc = dev_alloc(ctx, &B->B, mk * kp)) ||
+      (rc = dev_alloc(ctx, &B->XR, n * kp)) || (rc = dev_alloc(ctx, &B->stage, big * kp)) ||
+      (rc = dev_alloc(ctx, &B->Uf, mk * kp)) || (rc = dev_alloc(ctx, &B->Vf, n * kp)))
+    return rc;
+  CK(cudaMemsetAsync(B->U, 0, sizeof(double) * m * kp, ctx->stream));
+  CK(cudaMemsetAsync(B->V, 0, sizeof(double) * n * kp, ctx->stream));
+  CK(cudaMemsetAsync(B->Uf, 0, sizeof(float) * mk * kp, ctx->stream));
+  CK(cudaMemsetAsync(B->Vf, 0, sizeof(float) * n * kp, ctx->stream));
+  B->kp = kp;
+  return PLSQR_OK;
+}
+
+static int batch_setup(plsqr_ctx *ctx) {
+  int rc;
+  {
+    BatchState *B = ctx->batch;
+    if ((rc = dev_alloc(ctx, &B->k_hi, (size_t)ctx->nnz_k)) ||
+        (rc = dev_alloc(ctx, &B->kc_hi, (size_t)ctx->nnz_k)) ||
+        (rc = dev_alloc(ctx, &B->st, kBatchMax)) || (rc = dev_alloc(ctx, &B->cf, 1)) ||
+        (rc = dev_alloc(ctx, &B->LAM, kBatchMax)))
+      return rc;
+    B->own_hi = true;
+    const int g = ctx->sm_count * 8;
+    k_split_hilo<<<g, 256, 0, ctx->stream>>>(ctx->K.val, ctx->nnz_k, B->k_hi, nullptr);
+    k_split_hilo<<<g, 256, 0, ctx->stream>>>(ctx->KC.val, ctx->nnz_k, B->kc_hi, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(B->cf, 0, sizeof(BatchCoef), ctx->stream));
+    const std::vector<double> ones(kBatchMax, 1.0);
+    CK(cudaMemcpy(B->LAM, ones.data(), sizeof(double) * kBatchMax, cudaMemcpyHostToDevice));
+    // grids: four resident blocks of 256 threads per SM for the products
+    // (their launch bounds), one block per SM on the damping rows
+    B->gk = 4 * ctx->sm_count;
+    B->gd = ctx->sm_count;
+    B->gc = 4 * ctx->sm_count;
+    B->gres = 8 * ctx->sm_count;
+    B->gvec = 8 * ctx->sm_count;
+    std::vector<int64_t> kr((size_t)ctx->m_k + 1), kc((size_t)ctx->n + 1), dc((size_t)ctx->n + 1);
+    CK(cudaMemcpy(kr.data(), ctx->K.ptr, sizeof(int64_t) * kr.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(kc.data(), ctx->KC.ptr, sizeof(int64_t) * kc.size(), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(dc.data(), ctx->DC.ptr, sizeof(int64_t) * dc.size(), cudaMemcpyDeviceToHost));
+    B->shape = "r" + length_signature(kr) + "c" + length_signature(kc);
+    std::vector<int64_t> pre((size_t)ctx->n + 1);
+    for (size_t c = 0; c < pre.size(); ++c) pre[c] = kc[c] + (dc[c] - dc[0]);
+    std::vector<int32_t> wr, wc;
+    nnz_partition(kr, B->gk * (kBatchThreads / 32), wr);
+    nnz_partition(pre, B->gc * (kBatchThreads / 32), wc);
+    const int np = std::max(std::max(B->gk + B->gd, B->gc), std::max(B->gres, B->gvec));
+    if ((rc = dev_alloc(ctx, &B->wrows, wr.size())) || (rc = dev_alloc(ctx, &B->wcols, wc.size())) ||
+        (rc = dev_alloc(ctx, &B->parts, (size_t)np * kBatchMax)) ||
+        (rc = dev_alloc(ctx, &B->parts_dk, (size_t)np * kBatchMax)) ||
+        (rc = dev_alloc(ctx, &B->parts_err, (size_t)np * kBatchMax)))
+      return rc;
+    CK(cudaMemcpy(B->wrows, wr.data(), sizeof(int32_t) * wr.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B->wcols, wc.data(), sizeof(int32_t) * wc.size(), cudaMemcpyHostToDevice));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return PLSQR_OK;
+}
+
+// ---- variant choice ---------------------------------------------------------
+static int time_product(plsqr_ctx *ctx, BatchState *B, LaunchFn f, int mode, int reps,
+                        double *ms) {
+  f(ctx, *B, mode, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int i = 0; i < reps; ++i) f(ctx, *B, mode, ctx->stream);
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaGetLastError());
+  CK(cudaEventSynchronize(ctx->ev1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+  *ms = (double)t / reps;
+  return PLSQR_OK;
+}
+
+// Variants of the two products for the current block width: the requested
+// ones, else the cached choice for this operator shape and width, else the
+// fastest of the candidates timed here (plain products, a few launches each).
+static int batch_choose(plsqr_ctx *ctx, int want_rows, int want_cols) {
+  BatchState *B = ctx->batch;
+  const std::string key = B->shape + "|" + std::to_string(B->kw);
+  B->tuned = 0;
+  int vr = want_rows, vc = want_cols;
+  if (vr < 0 || vc < 0) {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      if (vr < 0) vr = it->second.first;
+      if (vc < 0) vc = it->second.second;
+    }
+  }
+  int rc;
+  double best_r = 1e30, best_c = 1e30;
+  if (vr < 0 || vc < 0) {
+    for (int v = 0; v < kNumVariants; ++v) {
+      if (!variant_ok(v, B->kw)) continue;
+      double t;
+      if (vr < 0) {
+        if ((rc = time_product(ctx, B, kVariants[v].rows, kScaleOne, 3, &t))) return rc;
+        if (t < best_r) best_r = t, B->var_rows = v;
+      }
+      if (vc < 0) {
+        if ((rc = time_product(ctx, B, kVariants[v].cols, kScaleOne, 3, &t))) return rc;
+        if (t < best_c) best_c = t, B->var_cols = v;
+      }
+    }
+    if (vr < 0) vr = B->var_rows, B->ms_rows = best_r;
+    if (vc < 0) vc = B->var_cols, B->ms_cols = best_c;
+    B->tuned = 1;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = std::make_pair(vr, vc);
+  }
+  B->var_rows = vr;
+  B->var_cols = vc;
+  return PLSQR_OK;
+}
+
+// ---- one inner iteration ------------------------------------------------------
+static int enqueue_iteration(plsqr_ctx *ctx, BatchState *B, cudaStream_t s) {
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  kVariants[B->var_rows].rows(ctx, *B, kScaleNegAlpha, s);
+  k_bscale_u<<<B->gvec, kBatchThreads, 0, s>>>(B->U, B->Uf, ctx->m_k, m, B->kw, B->cf);
+  kVariants[B->var_cols].cols(ctx, *B, kScaleNegBeta, s);
+  k_bupdate<<<B->gvec, kBatchThreads, 0, s>>>(B->V, B->Vf, B->W, B->DX, B->X,
+                                               B->has_ref ? B->XR : nullptr, ctx->n, B->kw, B->k,
+                                               B->cf, B->st, B->parts_dk, B->parts_err, 0, B->hist,
+                                               B->hist_stride);
+  CK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
+static int ensure_graph(plsqr_ctx *ctx, BatchState *B) {
+  char key[256];
+  snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%p/%d", B->var_rows, B->var_cols, B->kw, B->k,
+           (int)B->has_ref, (void *)B->hist, B->hist_stride);
+  if (B->graph && B->graph_key == key) return PLSQR_OK;
+  if (B->graph) cudaGraphExecDestroy(B->graph);
+  B->graph = nullptr;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_iteration(ctx, B, ctx->stream);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  CK(e);
+  e = cudaGraphInstantiate(&B->graph, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  B->graph_key = key;
+  return PLSQR_OK;
+}
+
+// ---- C ABI ----------------------------------------------------------------------
+extern "C" void plsqr_default_batch_args(plsqr_batch_args *a) {
+  if (!a) return;
+  memset(a, 0, sizeof(*a));
+  a->k = 1;
+  a->sweeps = 4;
+  a->inner = 50;
+  a->variant_rows = -1;
+  a->variant_cols = -1;
+  a->atol = 1e-10;  // source/lsqr.c:47-51
+  a->btol = 1e-10;
+  a->conlim = 100;
+}
+
+extern "C" int plsqr_batch_variant(int32_t index, int32_t *vw, int32_t *lanes_per_line,
+                                   int32_t *unroll) {
+  if (index < 0 || index >= kNumVariants) return PLSQR_ERR_ARG;
+  if (vw) *vw = kVariants[index].vw;
+  if (lanes_per_line) *lanes_per_line = kVariants[index].lpr;
+  if (unroll) *unroll = kVariants[index].u;
+  return PLSQR_OK;
+}
+
+static void fill_info(const BatchState *B, plsqr_batch_info *info) {
+  if (!info) return;
+  memset(info, 0, sizeof(*info));
+  info->k = B->k;
+  info->kp = B->kw;
+  info->variant_rows = B->var_rows;
+  info->variant_cols = B->var_cols;
+  info->tuned = B->tuned;
+  info->ms_rows = B->ms_rows;
+  info->ms_cols = B->ms_cols;
+}
+
+extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, double *x,
+                                plsqr_iter *hist, plsqr_result *res, plsqr_batch_info *info) {
+  if (!ctx || !a || !a->b_k) return PLSQR_ERR_ARG;
+  if (a->k < 1 || a->k > kBatchMax || a->sweeps < 1 || a->inner < 1) return PLSQR_ERR_ARG;
+  const int k = a->k, kw = width_for(k);
+  if ((a->variant_rows >= 0 && !variant_ok(a->variant_rows, kw)) ||
+      (a->variant_cols >= 0 && !variant_ok(a->variant_cols, kw)) ||
+      a->variant_rows >= kNumVariants || a->variant_cols >= kNumVariants)
+    return PLSQR_ERR_ARG;
+  if (a->lambda)
+    for (int j = 0; j < k; ++j)
+      if (!(a->lambda[j] >= 0.0) || a->lambda[j] > 1e300) return PLSQR_ERR_ARG;
+  const int S = a->sweeps, I = a->inner;
+  const int64_t total = (int64_t)S * I;
+  if (total > (int64_t)1 << 24) return PLSQR_ERR_ARG;
+  CK(cudaSetDevice(ctx->opts.device));
+  int rc;
+  if ((rc = batch_prepare(ctx, kw))) return rc;
+  BatchState *B = ctx->batch;
+  B->k = k;
+  B->kw = kw;
+  B->has_ref = a->x_ref != nullptr;
+  const int64_t n = ctx->n, mk = ctx->m_k, m = mk + ctx->m_d;
+  cudaStream_t s = ctx->stream;
+  // inputs: right-hand sides, weights, reference solutions
+  std::vector<double> lam(kBatchMax, 1.0);
+  for (int j = 0; j < k; ++j) lam[(size_t)j] = a->lambda ? a->lambda[j] : 1.0;
+  CK(cudaMemcpyAsync(B->LAM, lam.data(), sizeof(double) * kBatchMax, cudaMemcpyHostToDevice, s));
+  const int gl = 8 * ctx->sm_count;
+  if (mk > 0) {
+    CK(cudaMemcpyAsync(B->stage, a->b_k, sizeof(double) * mk * k, cudaMemcpyHostToDevice, s));
+    k_bgather<<<gl, 256, 0, s>>>(B->stage, mk, mk, kw, k, B->B);
+  }
+  if (a->x_ref) {
+    CK(cudaMemcpyAsync(B->stage, a->x_ref, sizeof(double) * n * k, cudaMemcpyHostToDevice, s));
+    k_bgather<<<gl, 256, 0, s>>>(B->stage, n, n, kw, k, B->XR);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(B->X, 0, sizeof(double) * n * kw, s));
+  // history: [k][total + 1]
+  B->hist_stride = (int)(total + 1);
+  if (B->hist_cap < (int64_t)k * (total + 1)) {
+    if (B->hist) dev_free(ctx, B->hist);
+    B->hist = nullptr;
+    B->hist_cap = 0;
+    if ((rc = dev_alloc(ctx, &B->hist, (size_t)k * (total + 1)))) return rc;
+    B->hist_cap = (int64_t)k * (total + 1);
+  }
+  CK(cudaMemsetAsync(B->hist, 0, sizeof(plsqr_iter) * k * (total + 1), s));
+  if ((rc = batch_choose(ctx, a->variant_rows, a->variant_cols))) return rc;
+  if ((rc = ensure_graph(ctx, B))) return rc;
+  std::vector<plsqr_iter> h0((size_t)k);
+  std::vector<DevState> cur((size_t)k);
+  memset(h0.data(), 0, sizeof(plsqr_iter) * k);
+  int last_itn = 0;
+  CK(cudaEventRecord(ctx->ev0, s));
+  for (int sw = 0; sw < S; ++sw) {
+    std::vector<DevState> h((size_t)k);
+    memset(h.data(), 0, sizeof(DevState) * k);
+    for (int j = 0; j < k; ++j) {
+      DevState &d = h[(size_t)j];
+      d.damp = a->damp;
+      d.atol = a->atol;
+      d.btol = a->btol;
+      d.ctol = a->conlim > 0.0 ? 1.0 / a->conlim : 0.0;
+      d.itnlim = (int32_t)std::min<int64_t>(total + 1, INT32_MAX);
+      d.has_ref = B->has_ref;
+      d.cs2 = -1.0;
+      d.hist_base = sw * I;
+    }
+    CK(cudaMemcpyAsync(B->st, h.data(), sizeof(DevState) * k, cudaMemcpyHostToDevice, s));
+    if (B->has_ref)
+      k_bref_norm<<<B->gvec, kBatchThreads, 0, s>>>(B->XR, ctx->n, kw, k, B->st, B->cf, B->parts);
+    // outer residual and the start-up of the correction solves
+    k_bresidual<<<B->gres, kBatchThreads, 0, s>>>(ctx->K.csr(), ctx->D.csr(), kw, k, B->X, B->B,
+                                                   B->U, B->LAM, B->st, B->cf, B->parts);
+    k_bscale_u<<<B->gvec, kBatchThreads, 0, s>>>(B->U, B->Uf, mk, m, kw, B->cf);
+    CK(cudaMemsetAsync(B->V, 0, sizeof(double) * n * kw, s));
+    kVariants[B->var_cols].cols(ctx, *B, kScaleZero, s);
+    k_bupdate<<<B->gvec, kBatchThreads, 0, s>>>(B->V, B->Vf, B->W, B->DX, B->X, nullptr, ctx->n,
+                                                 kw, k, B->cf, B->st, B->parts_dk, B->parts_err,
+                                                 1, nullptr, 1);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * k, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    bool all_done = true;
+    for (int j = 0; j < k; ++j) {
+      const DevState &c = cur[(size_t)j];
+      all_done = all_done && c.done;
+      if (sw == 0) {
+        plsqr_iter &e = h0[(size_t)j];
+        e.alpha = c.alpha;
+        e.beta = c.beta;
+        e.rnorm = c.beta;
+        e.arnorm = c.arnorm;
+        e.test1 = 1.0;
+        e.test2 = c.beta > 0.0 ? c.alpha / c.beta : 0.0;
+        e.err = B->has_ref ? 1.0 : -1.0;
+      }
+    }
+    if (all_done) break;  // A^T r_j = 0 for every j: X solves every problem
+    for (int i = 0; i < I; ++i) CK(cudaGraphLaunch(B->graph, s));
+    k_badd<<<gl, 256, 0, s>>>(B->X, B->DX, n * kw);
+    CK(cudaGetLastError());
+    last_itn = (sw + 1) * I;
+  }
+  CK(cudaEventRecord(ctx->ev1, s));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * k, cudaMemcpyDeviceToHost, s));
+  if (hist) {
+    CK(cudaMemcpyAsync(hist, B->hist, sizeof(plsqr_iter) * k * (total + 1), cudaMemcpyDeviceToHost,
+                       s));
+  }
+  if (x) {
+    k_bscatter<<<gl, 256, 0, s>>>(B->X, n, kw, k, B->stage, n);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(x, B->stage, sizeof(double) * n * k, cudaMemcpyDeviceToHost, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  if (hist)
+    for (int j = 0; j < k; ++j) hist[(int64_t)j * (total + 1)] = h0[(size_t)j];
+  if (res) {
+    for (int j = 0; j < k; ++j) {
+      const DevState &c = cur[(size_t)j];
+      plsqr_result &r = res[j];
+      memset(&r, 0, sizeof(r));
+      r.istop = c.istop;
+      r.itn = last_itn;
+      r.anorm = c.anorm;
+      r.acond = c.acond;
+      r.rnorm = c.rnorm;
+      r.arnorm_out = c.test2;
+      r.xnorm = c.xnorm;
+      r.arnorm = c.arnorm;
+      r.bnorm = c.bnorm;
+      r.dxmax = c.dxmax;
+      r.maxdx = c.maxdx;
+      r.seconds = ms * 1e-3;
+      r.seconds_total = r.seconds;
+    }
+  }
+  fill_info(B, info);
+  return PLSQR_OK;
+}
+
+extern "C" int plsqr_batch_bench_aprod(plsqr_ctx *ctx, int32_t k, int mode, int32_t variant,
+                                       int reps, double *ms_per_launch) {
+  if (!ctx || !ms_per_launch || k < 1 || k > kBatchMax || (mode != 1 && mode != 2) || reps < 1)
+    return PLSQR_ERR_ARG;
+  const int kw = width_for(k);
+  if (variant >= 0 && !variant_ok(variant, kw)) return PLSQR_ERR_ARG;
+  if (variant >= kNumVariants) return PLSQR_ERR_ARG;
+  CK(cudaSetDevice(ctx->opts.device));
+  int rc;
+  if ((rc = batch_prepare(ctx, kw))) return rc;
+  BatchState *B = ctx->batch;
+  B->k = k;
+  B->kw = kw;
+  if (variant < 0) {
+    if ((rc = batch_choose(ctx, -1, -1))) return rc;
+    variant = mode == 1 ? B->var_rows : B->var_cols;
+  }
+  const Variant &V = kVariants[variant];
+  return time_product(ctx, B, mode == 1 ? V.rows : V.cols, kScaleOne, reps, ms_per_launch);
+}
+
+// ---- damping weight ---------------------------------------------------------------
+static __global__ void k_weighted(const double *__restrict__ src, int64_t n, double w,
+                                  double *__restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = w == 1.0 ? src[i] : __dmul_rn(w, src[i]);
+}
+
+extern "C" int plsqr_set_damping_weight(plsqr_ctx *ctx, double lambda) {
+  if (!ctx || !(lambda >= 0.0) || lambda > 1e300) return PLSQR_ERR_ARG;
+  CK(cudaSetDevice(ctx->opts.device));
+  int rc;
+  if (!ctx->d_val0) {
+    if ((rc = dev_alloc(ctx, &ctx->d_val0, (size_t)ctx->nnz_d)) ||
+        (rc = dev_alloc(ctx, &ctx->dc_val0, (size_t)ctx->nnz_d)))
+      return rc;
+    CK(cudaMemcpyAsync(ctx->d_val0, ctx->D.val, sizeof(double) * ctx->nnz_d,
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->dc_val0, ctx->DC.val, sizeof(double) * ctx->nnz_d,
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  const int g = 4 * ctx->sm_count;
+  k_weighted<<<g, 256, 0, ctx->stream>>>(ctx->d_val0, ctx->nnz_d, lambda, ctx->D.val);
+  k_weighted<<<g, 256, 0, ctx->stream>>>(ctx->dc_val0, ctx->nnz_d, lambda, ctx->DC.val);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return PLSQR_OK;
+}

@@ -455,6 +455,7 @@ void plsqr_ctx_destroy(plsqr_ctx *ctx) {
   cudaSetDevice(ctx->opts.device);
   free_graph(ctx);
   mixed_free(ctx);
+  batch_free(ctx);
   for (auto &a : ctx->allocs) cudaFree(a.first);
   ctx->allocs.clear();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);

@@ -35,6 +35,7 @@ struct DevSlab {
 };
 
 struct MixedState;  // mixed.cu
+struct BatchState;  // batched.cu
 
 struct plsqr_ctx {
   plsqr_opts opts;
@@ -70,6 +71,8 @@ struct plsqr_ctx {
   int slab_group_f = 16;   // lanes per segment, FP32 slab products
   DevSlab<double> s_rows, s_cols;  // K by row (gathers v), K by column (gathers u_k)
   int gc1k = 1, gc1d = 1, gc2 = 1;  // grids of the combine kernels
+  BatchState *batch = nullptr;       // several right-hand sides (batched.cu)
+  double *d_val0 = nullptr, *dc_val0 = nullptr;  // damping values before weighting
 };
 
 // slab.cu
@@ -112,3 +115,6 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
 void mixed_free(plsqr_ctx *ctx);
 int mixed_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch);
 int mixed_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration);
+
+// batched.cu
+void batch_free(plsqr_ctx *ctx);

@@ -136,9 +136,9 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
     if (k < l1) {
       const int64_t g0 = ptr[l] >> 3, g1 = ptr[l + 1] >> 3;  // groups of 8 entries
       int64_t g = g0 + sub;
-      // FP64: two steps in flight; FP32 keeps one to stay within 32 registers
-      constexpr int kSteps = sizeof(T) == 8 ? 2 : 1;
-      for (; kSteps == 2 && g + kGroup < g1; g += 2 * kGroup) {
+      // two steps in flight; the FP32 build spills a few values at its 32
+      // registers per thread and still measured faster than one step
+      for (; g + kGroup < g1; g += 2 * kGroup) {
         const uint4 q = __ldg(idx8 + g), p = __ldg(idx8 + g + kGroup);
         T v[8], w[8];
         load8(A.val, g, v);

@@ -358,6 +358,17 @@ int plsqr_synth_xtrue(const plsqr_synth_params *P, double *x) {
   return 0;
 }
 
+// b = kx + noise_frac * rms(kx) * N(0,1), the normals drawn from `seed`
+// (b may be kx).
+static void add_noise(const double *kx, int64_t m, double noise_frac, uint64_t seed, double *b) {
+  double ss = 0.0;
+  for (int64_t r = 0; r < m; ++r) ss += kx[r] * kx[r];
+  const double rms = m > 0 ? sqrt(ss / (double)m) : 0.0;
+  const double sigma = noise_frac * rms;
+#pragma omp parallel for schedule(static)
+  for (int64_t r = 0; r < m; ++r) b[r] = kx[r] + sigma * det_normal(seed, kNoise, (uint64_t)r, 0);
+}
+
 int plsqr_synth_rhs(const plsqr_synth_params *P, const int64_t *row_ptr,
                     const int32_t *col_idx, const double *val, const double *xtrue,
                     double *b) {
@@ -370,12 +381,16 @@ int plsqr_synth_rhs(const plsqr_synth_params *P, const int64_t *row_ptr,
     for (int64_t e = row_ptr[r]; e < row_ptr[r + 1]; ++e) s += val[e] * xtrue[col_idx[e]];
     b[r] = s;
   }
-  double ss = 0.0;
-  for (int64_t r = 0; r < m; ++r) ss += b[r] * b[r];
-  const double rms = m > 0 ? sqrt(ss / (double)m) : 0.0;
-  const double sigma = P->noise_frac * rms;
-#pragma omp parallel for schedule(static)
-  for (int64_t r = 0; r < m; ++r) b[r] += sigma * det_normal(P->seed, kNoise, (uint64_t)r, 0);
+  add_noise(b, m, P->noise_frac, P->seed, b);
+  return 0;
+}
+
+int plsqr_synth_noisy(const plsqr_synth_params *P, uint64_t noise_seed, int64_t m,
+                      const double *kx, double *b) {
+  int rc = check_params(P);
+  if (rc) return rc;
+  if (m < 0 || (m > 0 && (!kx || !b))) return PLSQR_ERR_ARG;
+  add_noise(kx, m, P->noise_frac, noise_seed, b);
   return 0;
 }
 

@@ -160,6 +160,57 @@ class Context:
         res = {k: getattr(r, k) for k, _ in N.Result._fields_ if k != "pad"}
         return dict(x=x, w=w, se=se, hist=hist, result=res)
 
+    # -- several right-hand sides ----------------------------------------------
+    def batch_lsqr(self, b_k, *, lam=None, x_ref=None, sweeps: int = 4, inner: int = 50,
+                   damp: float = 0.0, atol: float = 1e-10, btol: float = 1e-10,
+                   conlim: float = 100.0, variant_rows: int = -1,
+                   variant_cols: int = -1) -> dict:
+        """k <= 32 solves in lock step, one k-wide product per matrix read.
+
+        b_k: (k, m_k) right-hand sides; lam: (k,) damping-row weights (solve j
+        uses [K; lam_j D]); x_ref: (k, n) solutions for the history's err
+        field.  Returns x (k, n), hist (k, sweeps*inner + 1), per-solve
+        results and the product variants used."""
+        b = np.ascontiguousarray(b_k, np.float64)
+        if b.ndim != 2 or b.shape[1] != self.m_k:
+            raise ValueError(f"b_k must have shape (k, {self.m_k}), got {b.shape}")
+        k = b.shape[0]
+        lm = None if lam is None else np.ascontiguousarray(lam, np.float64)
+        if lm is not None and lm.shape != (k,):
+            raise ValueError(f"lam must have {k} values")
+        xr = None if x_ref is None else np.ascontiguousarray(x_ref, np.float64)
+        if xr is not None and xr.shape != (k, self.n):
+            raise ValueError(f"x_ref must have shape ({k}, {self.n})")
+        a = N.BatchArgs()
+        N.lib().plsqr_default_batch_args(C.byref(a))
+        a.k, a.sweeps, a.inner = k, sweeps, inner
+        a.variant_rows, a.variant_cols = variant_rows, variant_cols
+        a.damp, a.atol, a.btol, a.conlim = damp, atol, btol, conlim
+        a.b_k, a.lambda_, a.x_ref = N.ptr(b), N.ptr(lm), N.ptr(xr)
+        x = np.empty((k, self.n))
+        hist = np.zeros((k, sweeps * inner + 1), N.ITER_DTYPE)
+        res = (N.Result * k)()
+        info = N.BatchInfo()
+        self._check(N.lib().plsqr_batch_lsqr(self._h, C.byref(a), N.ptr(x), N.ptr(hist),
+                                             C.cast(res, N.vp), C.byref(info)),
+                    "plsqr_batch_lsqr")
+        results = [{f: getattr(r, f) for f, _ in N.Result._fields_ if f != "pad"} for r in res]
+        return dict(x=x, hist=hist, results=results,
+                    info={f: getattr(info, f) for f, _ in N.BatchInfo._fields_ if f != "pad"})
+
+    def batch_bench_aprod(self, k: int, mode: int, variant: int = -1, reps: int = 5) -> float:
+        """ms per launch of the k-wide product (mode 1 or 2) of a variant
+        (-1: the one picked by timing)."""
+        ms = N.f64(0)
+        self._check(N.lib().plsqr_batch_bench_aprod(self._h, k, mode, variant, reps,
+                                                    C.byref(ms)), "plsqr_batch_bench_aprod")
+        return float(ms.value)
+
+    def set_damping_weight(self, lam: float) -> None:
+        """Damping rows become lam * D (from the values the context was made with)."""
+        self._check(N.lib().plsqr_set_damping_weight(self._h, float(lam)),
+                    "plsqr_set_damping_weight")
+
     # -- measurement ----------------------------------------------------------
     def bench_aprod(self, mode: int, reps: int = 10) -> float:
         """ms per launch of the mode-1/2 product kernel (overwrites u, v)."""

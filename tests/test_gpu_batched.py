@@ -1,0 +1,161 @@
+"""Batched right-hand sides (Context.batch_lsqr): k solves in lock step on one
+operator, one k-wide product per matrix read.
+
+There is no batched solver in the reference; the yardstick of every solve is
+the FP64 one-right-hand-side path (itself pinned to the reference), run on the
+same instance with the same damping weight."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def grid32(pkg, problems):
+    prob = problems("grid32")
+    with pkg.Context(prob) as ctx:
+        insts = pkg.batch.instances(ctx, prob, "grid32")
+    return prob, insts
+
+
+def fp64_solution(pkg, prob, inst, iterations):
+    with pkg.Context(prob) as c:
+        if inst.lam != 1.0:
+            c.set_damping_weight(inst.lam)
+        return c.lsqr(inst.b_k, lsqr_iteration=iterations)
+
+
+def test_instances_reach_their_fp64_solutions(pkg, grid32):
+    prob, insts = grid32
+    sel = pkg.batch.pick(insts, 6)
+    assert {i.name[:5] for i in sel} == {"noise", "lambd", "check"}
+    xstar = np.stack([fp64_solution(pkg, prob, i, 800)["x"] for i in sel])
+    with pkg.Context(prob) as ctx:
+        out = ctx.batch_lsqr(np.stack([i.b_k for i in sel]), lam=[i.lam for i in sel],
+                             x_ref=xstar, sweeps=5, inner=60)
+    for j, inst in enumerate(sel):
+        e = rel(out["x"][j], xstar[j])
+        assert e <= 1e-6, (inst.name, e)
+        err = out["hist"]["err"][j]
+        assert err[0] == 1.0
+        assert abs(err[-1] - e) <= 1e-3 * e + 1e-12, inst.name
+
+
+def test_columns_are_independent(pkg, grid32):
+    """A right-hand side gives the same bits alone and in a batch of the same
+    block width and product variants."""
+    prob, insts = grid32
+    sel = [insts[0], insts[16], insts[24]]
+    b = np.stack([i.b_k for i in sel])
+    lam = [i.lam for i in sel]
+    kw = dict(sweeps=2, inner=10, variant_rows=1, variant_cols=1)
+    with pkg.Context(prob) as ctx:
+        both = ctx.batch_lsqr(b, lam=lam, **kw)
+        for j in range(3):
+            one = ctx.batch_lsqr(b[j:j + 1], lam=lam[j:j + 1], **kw)
+            assert np.array_equal(one["x"][0], both["x"][j])
+            assert np.array_equal(one["hist"][0], both["hist"][j])
+
+
+def test_start_and_first_iteration_match_fp64(pkg, grid32):
+    prob, insts = grid32
+    sel = [insts[1], insts[20], insts[27]]
+    with pkg.Context(prob) as ctx:
+        out = ctx.batch_lsqr(np.stack([i.b_k for i in sel]), lam=[i.lam for i in sel],
+                             sweeps=1, inner=3)
+    for j, inst in enumerate(sel):
+        h64 = fp64_solution(pkg, prob, inst, 3)["hist"]
+        h = out["hist"][j]
+        assert h["beta"][0] == pytest.approx(np.linalg.norm(inst.b_k), rel=1e-14)
+        # FP32 kernel products: alpha and beta agree to FP32 accuracy
+        for f in ("alpha", "beta", "rnorm", "arnorm"):
+            assert np.allclose(h[f][:4], h64[f][:4], rtol=2e-5, atol=0), (inst.name, f)
+
+
+@pytest.mark.parametrize("k", [4, 32])
+def test_every_variant_gives_the_same_iterates(pkg, grid32, k):
+    prob, insts = grid32
+    sel = pkg.batch.pick(insts, k)
+    b = np.stack([i.b_k for i in sel])
+    lam = [i.lam for i in sel]
+    kw = 4 if k <= 4 else 32
+    ok = []
+    for v in range(64):
+        try:
+            vw, lpr, u = pkg._native.batch_variant(v)
+        except pkg._native.PlsqrError:
+            break
+        if kw % vw == 0 and kw // vw <= lpr:
+            ok.append(v)
+    assert len(ok) >= 6
+    with pkg.Context(prob) as ctx:
+        ref = ctx.batch_lsqr(b, lam=lam, sweeps=1, inner=6, variant_rows=ok[0],
+                             variant_cols=ok[0])
+        for v in ok[1:]:
+            out = ctx.batch_lsqr(b, lam=lam, sweeps=1, inner=6, variant_rows=v, variant_cols=v)
+            for f in ("alpha", "beta", "rnorm"):
+                assert np.allclose(out["hist"][f], ref["hist"][f], rtol=2e-5, atol=0), (v, f)
+            assert rel(out["x"], ref["x"]) <= 1e-4
+
+
+def test_tuning_is_cached_and_bench_runs(pkg, grid32):
+    prob, insts = grid32
+    # 12 right-hand sides: a block width (16) no other test here uses, so the
+    # process-wide choice is not cached yet
+    b = np.stack([i.b_k for i in insts[:12]])
+    with pkg.Context(prob) as ctx:
+        first = ctx.batch_lsqr(b, sweeps=1, inner=2)
+        assert first["info"]["tuned"] == 1 and first["info"]["kp"] == 16
+        assert first["info"]["ms_rows"] > 0 and first["info"]["ms_cols"] > 0
+        again = ctx.batch_lsqr(b, sweeps=1, inner=2)
+        assert again["info"]["tuned"] == 0
+        assert again["info"]["variant_rows"] == first["info"]["variant_rows"]
+        assert np.array_equal(again["x"], first["x"])
+        for mode in (1, 2):
+            assert ctx.batch_bench_aprod(12, mode, reps=2) > 0
+
+
+def test_zero_right_hand_side_stays_zero(pkg, grid32):
+    prob, insts = grid32
+    b = np.stack([insts[0].b_k, np.zeros(prob.m_k), insts[24].b_k])
+    with pkg.Context(prob) as ctx:
+        out = ctx.batch_lsqr(b, sweeps=2, inner=20)
+        alone = ctx.batch_lsqr(b[[0, 2]], sweeps=2, inner=20, variant_rows=out["info"][
+            "variant_rows"], variant_cols=out["info"]["variant_cols"])
+    assert np.all(out["x"][1] == 0.0)
+    assert np.all(np.isfinite(out["hist"]["rnorm"]))
+    assert np.array_equal(out["x"][[0, 2]], alone["x"])
+
+
+def test_batch_arguments_are_checked(pkg, grid32):
+    prob, insts = grid32
+    with pkg.Context(prob) as ctx:
+        for bad in (dict(b_k=np.zeros((33, prob.m_k))), dict(b_k=np.zeros((2, prob.m_k)),
+                                                            sweeps=0),
+                    dict(b_k=np.zeros((2, prob.m_k)), variant_rows=99),
+                    dict(b_k=np.zeros((2, prob.m_k)), lam=[1.0, -1.0])):
+            b = bad.pop("b_k")
+            with pytest.raises(pkg._native.PlsqrError) as e:
+                ctx.batch_lsqr(b, **bad)
+            assert e.value.code == -1
+        # a variant too narrow for the block: float2 gathers of 32 columns on
+        # 8 lanes
+        narrow = [v for v in range(12) if pkg._native.batch_variant(v) == (2, 8, 1)]
+        with pytest.raises(pkg._native.PlsqrError):
+            ctx.batch_lsqr(np.zeros((32, prob.m_k)), variant_rows=narrow[0])
+
+
+def test_damping_weight_round_trip(pkg, problems):
+    prob = problems("grid32")
+    with pkg.Context(prob) as c:
+        ref = c.lsqr(lsqr_iteration=20)
+        c.set_damping_weight(3.0)
+        w3 = c.lsqr(lsqr_iteration=20)
+        c.set_damping_weight(1.0)
+        back = c.lsqr(lsqr_iteration=20)
+    assert np.array_equal(ref["x"], back["x"])
+    assert not np.array_equal(ref["x"], w3["x"])
