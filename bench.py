@@ -172,10 +172,23 @@ def main() -> int:
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: build the context, run one short solve, exit")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--extension", default=None, choices=["batched", "uneven"],
+                    help="measure an extension instead: 32 right-hand sides on the "
+                         "96x96x32 operator, or the 24 uneven problems in one launch")
+    ap.add_argument("--variant-rows", type=int, default=-1,
+                    help="batched product variant of A x (-1: pick by timing)")
+    ap.add_argument("--variant-cols", type=int, default=-1,
+                    help="batched product variant of A^T y (-1: pick by timing)")
     args = ap.parse_args()
 
     ws, rank, local = dist()
     pkg = graft.load_package()
+    if args.extension and not args.profile:
+        if rank != 0:
+            return 0
+        fn = bench_batched if args.extension == "batched" else bench_uneven
+        print(json.dumps(fn(pkg, args, local)))
+        return 0
     cfg = pkg.CONFIGS[args.config]
     iters = args.iterations or cfg["iterations"]
 
@@ -210,6 +223,21 @@ def main() -> int:
         print(json.dumps(line))
         return 0
 
+    if args.profile and args.extension == "batched":
+        prob = pkg.generate(args.config)
+        with pkg.Context(prob, device=local) as ctx:
+            insts = pkg.batch.instances(ctx, prob, args.config)
+            out = ctx.batch_lsqr(np.stack([i.b_k for i in insts]), lam=[i.lam for i in insts],
+                                 sweeps=1, inner=2, variant_rows=args.variant_rows,
+                                 variant_cols=args.variant_cols)
+        log(f"profile run: {args.config}, 32 right-hand sides, variants {out['info']}")
+        return 0
+    if args.profile and args.extension == "uneven":
+        probs = [pkg.generate(c) for c in pkg.multi.uneven_configs()]
+        with pkg.multi.Multi(probs, device=local) as mp:
+            out = mp.solve()
+        log(f"profile run: 24 uneven problems, {out['seconds'] * 1e3:.2f} ms")
+        return 0
     if args.profile:
         prob = pkg.generate(args.config)
         with pkg.Context(prob, device=local, precision=args.precision) as ctx:
@@ -352,6 +380,122 @@ def time_to_tol(pkg, prob, ctx64, iters, tol) -> dict:
         else:
             out["mixed"] = {"sweeps": None, "final_err": float(hm["err"][-1])}
     return out
+
+
+# ---- extensions ---------------------------------------------------------------------
+def bench_batched(pkg, args, device) -> dict:
+    """32 right-hand sides on the 96x96x32 operator (16 noise seeds, 8 damping
+    weights, 8 checkerboards): time until every one is within 1e-6 of its own
+    FP64 solution, batched (one k=32 solve) against the plain FP64 path run
+    once per right-hand side."""
+    tol = 1e-6
+    name = args.config
+    iters = args.iterations or pkg.CONFIGS[name]["iterations"]
+    prob = pkg.generate(name)
+    ctx = pkg.Context(prob, device=device)
+    insts = pkg.batch.instances(ctx, prob, name)
+    ms_it = None
+    per = []
+    xstar = []
+    for inst in insts:
+        ctx.set_damping_weight(inst.lam)
+        xs = ctx.lsqr(inst.b_k, lsqr_iteration=2 * iters)["x"]
+        ctx.set_reference_x(xs)
+        h = ctx.lsqr(inst.b_k, lsqr_iteration=2 * iters)["hist"]
+        ctx.set_reference_x(None)
+        if ms_it is None:
+            ms_it = ctx.bench_iteration(reps=20)
+        k = first_below(h["err"], tol)
+        per.append({"name": inst.name, "lambda": inst.lam, "fp64_iterations": k})
+        xstar.append(xs)
+        log(f"{inst.name}: FP64 reaches {tol:g} at {k}")
+    ctx.set_damping_weight(1.0)
+    # plain FP64, one solve per right-hand side: iterations x graph-replayed
+    # iteration time, plus the start-up (a plain solve of 0 iterations)
+    t0 = ctx.lsqr(insts[0].b_k, lsqr_iteration=1)["result"]
+    startup = max(t0["seconds_total"] - t0["seconds"], 0.0)
+    b = np.stack([i.b_k for i in insts])
+    lam = [i.lam for i in insts]
+    X = np.stack(xstar)
+    inner = 2 * iters
+    tr = ctx.batch_lsqr(b, lam=lam, x_ref=X, sweeps=2, inner=inner)
+    ks = [first_below(tr["hist"]["err"][j], tol) for j in range(len(insts))]
+    for p, k, h in zip(per, ks, tr["hist"]["err"]):
+        p["batched_iterations"] = k
+        p["batched_final_err"] = float(h[-1])
+    # instances whose FP64 path only reaches the tolerance near the end of the
+    # reference run have no converged reference solution: reported, not timed
+    ok = [p["fp64_iterations"] is not None and p["fp64_iterations"] < 1.9 * iters for p in per]
+    for p, o in zip(per, ok):
+        p["timed"] = bool(o)
+    out = {"metric": "time to 1e-6 rel. error for 32 right-hand sides (vs each one's FP64 "
+                     "solution)", "unit": "s", "higher_is_better": False,
+           "extension": "batched", "n_gpus": 1, "dtype": "f32 products / f64 vectors",
+           "data": "synthetic (seeded generator)",
+           "config": {"workload": f"{name}: 32 right-hand sides (16 noise seeds, 8 damping "
+                                  f"weights 0.1-10, 8 checkerboards period 4-16)",
+                      "m_k": prob.m_k, "n": prob.n, "nnz_k": prob.meta["nnz_k"],
+                      "reference_solutions": f"FP64 LSQR, {2 * iters} iterations each"},
+           "instances": per, "variants": tr["info"]}
+    if all(k is not None for k, o in zip(ks, ok) if o):
+        K = max(k for k, o in zip(ks, ok) if o)
+        fp64_total = sum(startup + p["fp64_iterations"] * ms_it * 1e-3
+                         for p, o in zip(per, ok) if o)
+        sweeps = (K - 1) // inner + 1
+        run = dict(sweeps=1, inner=K) if sweeps == 1 else dict(sweeps=sweeps, inner=inner)
+        t = [ctx.batch_lsqr(b, lam=lam, **run)["results"][0]["seconds"] for _ in range(2)]
+        out.update(value=min(t), run=run, timed_instances=int(sum(ok)),
+                   fp64_sequential_seconds=fp64_total,
+                   speedup_vs_fp64_sequential=fp64_total / min(t),
+                   note="value: the batched solve (all 32 right-hand sides) run until every "
+                        "timed instance is within the tolerance; fp64_sequential_seconds: "
+                        "the timed instances one after another on the plain FP64 path")
+    else:
+        out.update(value=None, note="not every right-hand side reached the tolerance")
+    ms1 = ctx.batch_bench_aprod(32, 1, reps=3)
+    ms2 = ctx.batch_bench_aprod(32, 2, reps=3)
+    nk = prob.meta["nnz_k"]
+    out["products"] = {"ms_ax": ms1, "ms_aty": ms2, "fp64_iteration_ms": ms_it,
+                       "gather_bytes_per_product": 128.0 * nk,
+                       "gather_tb_s": {"ax": 128.0 * nk / ms1 / 1e9, "aty": 128.0 * nk / ms2 / 1e9},
+                       "matrix_gb_s": {"ax": 8.0 * nk / ms1 / 1e6, "aty": 8.0 * nk / ms2 / 1e6}}
+    ctx.close()
+    return out
+
+
+def bench_uneven(pkg, args, device) -> dict:
+    """The 24 uneven problems (16^3-64^3 grids, 500-20,000 rays, 100 FP64 LSQR
+    iterations each): one persistent launch against one plain solve per
+    problem (each with its own graph-replayed iterations) on the same GPU."""
+    probs = [pkg.generate(c) for c in pkg.multi.uneven_configs()]
+    with pkg.multi.Multi(probs, device=device) as mp:
+        for _ in range(max(args.warmup, 1)):
+            mp.solve()
+        t = []
+        for _ in range(max(args.steps, 1)):
+            out = mp.solve()
+            t.append(out["seconds"])
+        info = mp.info()
+        g, gb = mp.plan()
+    seq, worst = 0.0, 0.0
+    for p, x in zip(probs, out["x"]):
+        with pkg.Context(p, device=device) as c:
+            c.lsqr(lsqr_iteration=p.iterations)
+            r = min((c.lsqr(lsqr_iteration=p.iterations) for _ in range(2)),
+                    key=lambda r: r["result"]["seconds_total"])
+        seq += r["result"]["seconds_total"]
+        worst = max(worst, float(np.linalg.norm(x - r["x"]) / np.linalg.norm(r["x"])))
+    its = sum(p.iterations for p in probs)
+    return {"metric": "24 uneven FP64 LSQR problems (100 iterations each) in one persistent "
+                      "launch: device time", "unit": "s", "value": min(t),
+            "higher_is_better": False, "extension": "uneven", "n_gpus": 1, "dtype": "f64",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "24 problems: grids 16^3-64^3, 500-20000 rays, tube radius "
+                                   "1.5", "nnz_k": [p.meta["nnz_k"] for p in probs],
+                       "blocks": info["blocks"], "blocks_per_problem": gb[g].tolist()},
+            "sequential_seconds": seq, "speedup_vs_sequential": seq / min(t),
+            "problem_iterations_per_s": its / min(t),
+            "max_rel_diff_vs_one_problem_path": worst}
 
 
 if __name__ == "__main__":

@@ -255,7 +255,9 @@ typedef struct {
 void plsqr_default_batch_args(plsqr_batch_args *a);
 
 /* Product variants: kVW-wide gathers (4 = float4, 2 = float2), kLPR lanes per
- * line, kU nonzeros in flight per lane.  Returns PLSQR_ERR_ARG past the last. */
+ * line, kU nonzeros in flight per lane; kLPR = 0 is the slab form (the
+ * gathered block staged through shared memory a slab at a time, kw/4 lanes
+ * per line).  Returns PLSQR_ERR_ARG past the last. */
 int plsqr_batch_variant(int32_t index, int32_t *vw, int32_t *lanes_per_line,
                         int32_t *unroll);
 
@@ -315,12 +317,24 @@ int plsqr_multi_info_get(const plsqr_multi *mp, plsqr_multi_info *info);
 /* The plan: group[p] of every problem and the blocks of every group
  * (arrays of count entries; group_blocks entries past info.groups are 0). */
 int plsqr_multi_plan(const plsqr_multi *mp, int32_t *group, int32_t *group_blocks);
+/* exact = 1: the products round every multiply and add apart, in the
+ * reference's order, so each row and column sum is the reference's to the
+ * bit (twice the FP64 instructions); 0 (default): fused multiply-adds in the
+ * same order. */
+int plsqr_multi_set_exact(plsqr_multi *mp, int32_t exact);
 /* Set the barrier wait limit (nanoseconds, >= 1000); default one second. */
 int plsqr_multi_set_wait(plsqr_multi *mp, int64_t wait_ns);
 /* Solve all problems.  x: the solutions one after another (sum of n_p
  * values) or NULL; hist: lsqr_iteration_p + 1 records per problem, one after
  * another, or NULL; res: [count] or NULL. */
 int plsqr_multi_solve(plsqr_multi *mp, double *x, plsqr_iter *hist, plsqr_result *res);
+/* The planner alone, on the host: problems with the given modelled bytes per
+ * iteration and iteration counts on `blocks` blocks of bw_block bytes/s
+ * each.  group[count]; group_blocks needs max(count, blocks) entries;
+ * *n_groups = groups made. */
+int plsqr_multi_plan_host(const double *bytes, const int32_t *iters, int32_t count,
+                          int32_t blocks, double bw_block, int32_t *group,
+                          int32_t *group_blocks, int32_t *n_groups);
 /* Runs one bounded wait on a flag that nothing sets, on the device, with the
  * given limit: returns PLSQR_ERR_TIMEOUT and leaves the context usable. */
 int plsqr_multi_check_wait(plsqr_multi *mp, int64_t wait_ns);

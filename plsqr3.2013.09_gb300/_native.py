@@ -81,6 +81,17 @@ class BatchInfo(C.Structure):
                 ("tuned", i32), ("pad", i32), ("ms_rows", f64), ("ms_cols", f64)]
 
 
+class ProblemDesc(C.Structure):
+    _fields_ = [("k_csc", Sparse), ("d_csr", Sparse), ("d_csc", Sparse), ("b_k", vp),
+                ("lsqr_iteration", i32), ("itnlim", i32), ("damp", f64), ("atol", f64),
+                ("btol", f64), ("conlim", f64)]
+
+
+class MultiInfo(C.Structure):
+    _fields_ = [("count", i32), ("blocks", i32), ("groups", i32), ("blocks_per_sm", i32),
+                ("device_bytes", i64), ("wait_ns", i64), ("seconds", f64)]
+
+
 ITER_DTYPE = np.dtype([(k, "<f8") for k in ("alpha", "beta", "rnorm", "arnorm", "test1", "test2",
                                              "anorm", "acond", "xnorm", "x0", "err")]
                       + [("istop", "<i4"), ("pad", "<i4")])
@@ -117,6 +128,17 @@ SIGNATURES = {
     "plsqr_batch_lsqr": (C.c_int, [vp, C.POINTER(BatchArgs), vp, vp, vp, C.POINTER(BatchInfo)]),
     "plsqr_batch_bench_aprod": (C.c_int, [vp, i32, C.c_int, i32, C.c_int, C.POINTER(f64)]),
     "plsqr_set_damping_weight": (C.c_int, [vp, f64]),
+    "plsqr_default_problem": (None, [C.POINTER(ProblemDesc)]),
+    "plsqr_multi_create": (C.c_int, [C.POINTER(ProblemDesc), i32, C.POINTER(Opts), C.POINTER(vp)]),
+    "plsqr_multi_destroy": (None, [vp]),
+    "plsqr_multi_last_error": (C.c_char_p, [vp]),
+    "plsqr_multi_info_get": (C.c_int, [vp, C.POINTER(MultiInfo)]),
+    "plsqr_multi_plan": (C.c_int, [vp, vp, vp]),
+    "plsqr_multi_plan_host": (C.c_int, [vp, vp, i32, i32, f64, vp, vp, C.POINTER(i32)]),
+    "plsqr_multi_set_wait": (C.c_int, [vp, i64]),
+    "plsqr_multi_set_exact": (C.c_int, [vp, i32]),
+    "plsqr_multi_solve": (C.c_int, [vp, vp, vp, vp]),
+    "plsqr_multi_check_wait": (C.c_int, [vp, i64]),
     "plsqr_io_read_kernel_info": (C.c_int, [C.c_char_p, i32, vp, vp, C.POINTER(i64)]),
     "plsqr_io_read_kernel": (C.c_int, [C.c_char_p, C.c_char_p, i32, i32, vp, vp, vp]),
     "plsqr_io_read_int32_counts": (C.c_int, [C.c_char_p, i64, vp, C.POINTER(i64)]),

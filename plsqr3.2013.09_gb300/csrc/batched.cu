@@ -76,6 +76,14 @@ struct BatchState {
   int hist_stride = 1;
   cudaGraphExec_t graph = nullptr;
   std::string graph_key;
+  // slab form: team slots and grids per block width
+  struct SlabPlan {
+    int32_t *rows = nullptr, *cols = nullptr;
+    int g_rows = 0, g_cols = 0;
+  };
+  std::map<int, SlabPlan> slab;
+  int n_parts = 0;          // capacity of parts (per right-hand side)
+  bool lines_sorted = true;  // every kernel row and column ascending (slab form)
 };
 
 namespace {
@@ -93,12 +101,48 @@ void launch_cols(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) 
       B.kw, B.k, B.Uf, B.U, ctx->m_k, B.V, B.LAM, mode, B.st, B.cf, B.parts);
 }
 
+template <int T>
+void launch_slab_rows_t(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  const BatchState::SlabPlan &P = B.slab.at(B.kw);
+  k_bslab_rows<T><<<P.g_rows, kSlabThreads, kSlabBytes, s>>>(
+      CsrT<float>{ctx->K.ptr, ctx->K.idx, B.k_hi, ctx->K.n_lines}, P.rows, ctx->n, B.k, B.Vf,
+      B.U, mode, B.st, B.parts);
+  k_bdamp_rows<<<B.gd, kBatchThreads, 0, s>>>(ctx->D.csr(), ctx->m_k, B.kw, B.k, B.V, B.U, B.LAM,
+                                              mode, B.st, B.cf, B.parts, P.g_rows);
+}
+template <int T>
+void launch_slab_cols_t(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  const BatchState::SlabPlan &P = B.slab.at(B.kw);
+  k_bslab_cols<T><<<P.g_cols, kSlabThreads, kSlabBytes, s>>>(
+      CsrT<float>{ctx->KC.ptr, ctx->KC.idx, B.kc_hi, ctx->KC.n_lines}, ctx->DC.csr(), P.cols,
+      ctx->m_k, B.k, B.Uf, B.U, B.V, B.LAM, mode, B.st, B.cf, B.parts);
+}
+void launch_slab_rows(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  switch (B.kw) {
+    case 4: return launch_slab_rows_t<1>(ctx, B, mode, s);
+    case 8: return launch_slab_rows_t<2>(ctx, B, mode, s);
+    case 16: return launch_slab_rows_t<4>(ctx, B, mode, s);
+    default: return launch_slab_rows_t<8>(ctx, B, mode, s);
+  }
+}
+void launch_slab_cols(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  switch (B.kw) {
+    case 4: return launch_slab_cols_t<1>(ctx, B, mode, s);
+    case 8: return launch_slab_cols_t<2>(ctx, B, mode, s);
+    case 16: return launch_slab_cols_t<4>(ctx, B, mode, s);
+    default: return launch_slab_cols_t<8>(ctx, B, mode, s);
+  }
+}
+
 #define VARIANT(vw, lpr, u) \
   Variant { vw, lpr, u, launch_rows<vw, lpr, u>, launch_cols<vw, lpr, u> }
+// lpr = 0: the slab form (float4 gathers from shared memory, kw/4 lanes per
+// line, kSlabLines lines per team)
 const Variant kVariants[] = {
     VARIANT(4, 8, 1),  VARIANT(4, 8, 2),  VARIANT(4, 16, 1), VARIANT(4, 16, 2),
     VARIANT(4, 32, 1), VARIANT(4, 32, 2), VARIANT(2, 16, 1), VARIANT(2, 16, 2),
     VARIANT(2, 32, 1), VARIANT(2, 32, 2), VARIANT(2, 8, 1),  VARIANT(2, 8, 2),
+    Variant{4, 0, 0, launch_slab_rows, launch_slab_cols},
 };
 #undef VARIANT
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
@@ -106,7 +150,30 @@ constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 bool variant_ok(int v, int kp) {
   if (v < 0 || v >= kNumVariants) return false;
   const Variant &V = kVariants[v];
+  if (V.lpr == 0) return true;
   return kp % V.vw == 0 && kp / V.vw <= V.lpr;
+}
+
+// Team slots of the slab form: lines dealt longest first to all teams in
+// turn, forward then backward (snake), so the teams' nonzero totals are
+// close; slots[(block*teams + team)*kSlabLines + t], -1 where none.
+int deal_lines(const std::vector<int64_t> &len, int teams_per_block, std::vector<int32_t> &slots) {
+  const int64_t n = (int64_t)len.size();
+  const int per_block = teams_per_block * kSlabLines;
+  const int grid = (int)std::max<int64_t>(1, (n + per_block - 1) / per_block);
+  const int64_t teams = (int64_t)grid * teams_per_block;
+  std::vector<int32_t> order((size_t)n);
+  for (int64_t i = 0; i < n; ++i) order[(size_t)i] = (int32_t)i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return len[(size_t)a] > len[(size_t)b]; });
+  slots.assign((size_t)teams * kSlabLines, -1);
+  int64_t next = 0;
+  for (int t = 0; t < kSlabLines && next < n; ++t)
+    for (int64_t i = 0; i < teams && next < n; ++i) {
+      const int64_t team = (t % 2 == 0) ? i : teams - 1 - i;
+      slots[(size_t)(team * kSlabLines + t)] = order[(size_t)next++];
+    }
+  return grid;
 }
 
 int width_for(int k) {
@@ -152,6 +219,19 @@ void nnz_partition(const std::vector<int64_t> &pre, int parts, std::vector<int32
 
 }  // namespace
 
+// flag = 1 if some line has its indices out of ascending order (the slab
+// form walks each line's entries as one ascending run).
+static __global__ void k_check_sorted(const int64_t *__restrict__ ptr,
+                                      const int32_t *__restrict__ idx, int n_lines,
+                                      int *__restrict__ flag) {
+  for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n_lines; l += gridDim.x * blockDim.x)
+    for (int64_t e = ptr[l] + 1; e < ptr[l + 1]; ++e)
+      if (idx[e] < idx[e - 1]) {
+        *flag = 1;
+        break;
+      }
+}
+
 void batch_free(plsqr_ctx *ctx) {
   if (!ctx || !ctx->batch) return;
   if (ctx->batch->graph) cudaGraphExecDestroy(ctx->batch->graph);
@@ -171,6 +251,7 @@ static void free_vectors(plsqr_ctx *ctx, BatchState *B) {
 // Device buffers for blocks of width kp, the FP32 kernel values and the
 // per-warp line ranges of the products.
 static int batch_setup(plsqr_ctx *ctx);
+
 
 static int batch_prepare(plsqr_ctx *ctx, int kp) {
   int rc;
@@ -237,7 +318,42 @@ static int batch_setup(plsqr_ctx *ctx) {
     std::vector<int32_t> wr, wc;
     nnz_partition(kr, B->gk * (kBatchThreads / 32), wr);
     nnz_partition(pre, B->gc * (kBatchThreads / 32), wc);
-    const int np = std::max(std::max(B->gk + B->gd, B->gc), std::max(B->gres, B->gvec));
+    int np = std::max(std::max(B->gk + B->gd, B->gc), std::max(B->gres, B->gvec));
+    // slab form: team slots for every block width
+    std::vector<int64_t> rl((size_t)ctx->m_k), cl((size_t)ctx->n);
+    for (int32_t r = 0; r < ctx->m_k; ++r) rl[(size_t)r] = kr[(size_t)r + 1] - kr[(size_t)r];
+    for (int32_t c = 0; c < ctx->n; ++c) cl[(size_t)c] = kc[(size_t)c + 1] - kc[(size_t)c];
+    for (int kw = 4; kw <= kBatchMax; kw *= 2) {
+      BatchState::SlabPlan P;
+      std::vector<int32_t> sr, sc;
+      P.g_rows = deal_lines(rl, kSlabThreads / (kw / 4), sr);
+      P.g_cols = deal_lines(cl, kSlabThreads / (kw / 4), sc);
+      if ((rc = dev_alloc(ctx, &P.rows, sr.size())) || (rc = dev_alloc(ctx, &P.cols, sc.size())))
+        return rc;
+      CK(cudaMemcpy(P.rows, sr.data(), sizeof(int32_t) * sr.size(), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(P.cols, sc.data(), sizeof(int32_t) * sc.size(), cudaMemcpyHostToDevice));
+      np = std::max(np, std::max(P.g_rows + B->gd, P.g_cols));
+      B->slab[kw] = P;
+    }
+    CK(cudaFuncSetAttribute(k_bslab_rows<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    CK(cudaFuncSetAttribute(k_bslab_rows<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    CK(cudaFuncSetAttribute(k_bslab_rows<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    CK(cudaFuncSetAttribute(k_bslab_rows<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    CK(cudaFuncSetAttribute(k_bslab_cols<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    CK(cudaFuncSetAttribute(k_bslab_cols<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    CK(cudaFuncSetAttribute(k_bslab_cols<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    CK(cudaFuncSetAttribute(k_bslab_cols<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSlabBytes));
+    B->n_parts = np;
+    int *flag = nullptr;
+    if ((rc = dev_alloc(ctx, &flag, 1))) return rc;
+    CK(cudaMemset(flag, 0, sizeof(int)));
+    k_check_sorted<<<ctx->sm_count * 8, 256>>>(ctx->K.ptr, ctx->K.idx, ctx->m_k, flag);
+    k_check_sorted<<<ctx->sm_count * 8, 256>>>(ctx->KC.ptr, ctx->KC.idx, ctx->n, flag);
+    CK(cudaGetLastError());
+    int h = 0;
+    CK(cudaMemcpy(&h, flag, sizeof(int), cudaMemcpyDeviceToHost));
+    dev_free(ctx, flag);
+    B->lines_sorted = h == 0;
     if ((rc = dev_alloc(ctx, &B->wrows, wr.size())) || (rc = dev_alloc(ctx, &B->wcols, wc.size())) ||
         (rc = dev_alloc(ctx, &B->parts, (size_t)np * kBatchMax)) ||
         (rc = dev_alloc(ctx, &B->parts_dk, (size_t)np * kBatchMax)) ||
@@ -286,7 +402,7 @@ static int batch_choose(plsqr_ctx *ctx, int want_rows, int want_cols) {
   double best_r = 1e30, best_c = 1e30;
   if (vr < 0 || vc < 0) {
     for (int v = 0; v < kNumVariants; ++v) {
-      if (!variant_ok(v, B->kw)) continue;
+      if (!variant_ok(v, B->kw) || (kVariants[v].lpr == 0 && !B->lines_sorted)) continue;
       double t;
       if (vr < 0) {
         if ((rc = time_product(ctx, B, kVariants[v].rows, kScaleOne, 3, &t))) return rc;
@@ -399,6 +515,11 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
   int rc;
   if ((rc = batch_prepare(ctx, kw))) return rc;
   BatchState *B = ctx->batch;
+  if (!B->lines_sorted && ((a->variant_rows >= 0 && kVariants[a->variant_rows].lpr == 0) ||
+                           (a->variant_cols >= 0 && kVariants[a->variant_cols].lpr == 0))) {
+    ctx_set_error(ctx, "the slab form needs every kernel row and column in ascending order");
+    return PLSQR_ERR_ARG;
+  }
   B->k = k;
   B->kw = kw;
   B->has_ref = a->x_ref != nullptr;
@@ -544,6 +665,7 @@ extern "C" int plsqr_batch_bench_aprod(plsqr_ctx *ctx, int32_t k, int mode, int3
     if ((rc = batch_choose(ctx, -1, -1))) return rc;
     variant = mode == 1 ? B->var_rows : B->var_cols;
   }
+  if (kVariants[variant].lpr == 0 && !B->lines_sorted) return PLSQR_ERR_ARG;
   const Variant &V = kVariants[variant];
   return time_product(ctx, B, mode == 1 ? V.rows : V.cols, kScaleOne, reps, ms_per_launch);
 }

@@ -37,10 +37,10 @@ def test_binding_covers_header(pkg):
 def test_struct_sizes_match_header(pkg):
     N = pkg._native
     # sizes the C compiler gives the header's structs (x86_64 and aarch64 LP64)
-    src = "#include <stdio.h>\n#include \"plsqr_gpu.h\"\nint main(){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\"," \
+    src = "#include <stdio.h>\n#include \"plsqr_gpu.h\"\nint main(){printf(\"%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n\"," \
           "sizeof(plsqr_sparse),sizeof(plsqr_files),sizeof(plsqr_opts),sizeof(plsqr_info)," \
           "sizeof(plsqr_lsqr_args),sizeof(plsqr_iter),sizeof(plsqr_result),sizeof(plsqr_synth_params),0," \
-          "sizeof(plsqr_batch_args),sizeof(plsqr_batch_info));}"
+          "sizeof(plsqr_batch_args),sizeof(plsqr_batch_info),sizeof(plsqr_problem),sizeof(plsqr_multi_info));}"
     import tempfile
     with tempfile.TemporaryDirectory() as d:
         (open(f"{d}/s.c", "w")).write(src)
@@ -48,7 +48,7 @@ def test_struct_sizes_match_header(pkg):
         sizes = list(map(int, subprocess.run([f"{d}/s"], capture_output=True, text=True).stdout.split()))
     mine = [C.sizeof(N.Sparse), C.sizeof(N.Files), C.sizeof(N.Opts), C.sizeof(N.Info),
             C.sizeof(N.LsqrArgs), N.ITER_DTYPE.itemsize, C.sizeof(N.Result), C.sizeof(N.SynthParams), 0,
-            C.sizeof(N.BatchArgs), C.sizeof(N.BatchInfo)]
+            C.sizeof(N.BatchArgs), C.sizeof(N.BatchInfo), C.sizeof(N.ProblemDesc), C.sizeof(N.MultiInfo)]
     assert sizes == mine
 
 

@@ -89,9 +89,9 @@ def test_every_variant_gives_the_same_iterates(pkg, grid32, k):
             vw, lpr, u = pkg._native.batch_variant(v)
         except pkg._native.PlsqrError:
             break
-        if kw % vw == 0 and kw // vw <= lpr:
+        if lpr == 0 or (kw % vw == 0 and kw // vw <= lpr):  # lpr 0: slab form
             ok.append(v)
-    assert len(ok) >= 6
+    assert len(ok) >= 7
     with pkg.Context(prob) as ctx:
         ref = ctx.batch_lsqr(b, lam=lam, sweeps=1, inner=6, variant_rows=ok[0],
                              variant_cols=ok[0])
@@ -144,7 +144,7 @@ def test_batch_arguments_are_checked(pkg, grid32):
             assert e.value.code == -1
         # a variant too narrow for the block: float2 gathers of 32 columns on
         # 8 lanes
-        narrow = [v for v in range(12) if pkg._native.batch_variant(v) == (2, 8, 1)]
+        narrow = [v for v in range(13) if pkg._native.batch_variant(v) == (2, 8, 1)]
         with pytest.raises(pkg._native.PlsqrError):
             ctx.batch_lsqr(np.zeros((32, prob.m_k)), variant_rows=narrow[0])
 
