@@ -139,9 +139,9 @@ void launch_slab_cols(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_
 // lpr = 0: the slab form (float4 gathers from shared memory, kw/4 lanes per
 // line, kSlabLines lines per team)
 const Variant kVariants[] = {
-    VARIANT(4, 8, 1),  VARIANT(4, 8, 2),  VARIANT(4, 16, 1), VARIANT(4, 16, 2),
-    VARIANT(4, 32, 1), VARIANT(4, 32, 2), VARIANT(2, 16, 1), VARIANT(2, 16, 2),
-    VARIANT(2, 32, 1), VARIANT(2, 32, 2), VARIANT(2, 8, 1),  VARIANT(2, 8, 2),
+    VARIANT(4, 8, 2),  VARIANT(4, 8, 4),  VARIANT(4, 16, 2), VARIANT(4, 16, 4),
+    VARIANT(4, 32, 2), VARIANT(4, 32, 4), VARIANT(2, 16, 2), VARIANT(2, 16, 4),
+    VARIANT(2, 32, 2), VARIANT(2, 32, 4), VARIANT(2, 8, 2),  VARIANT(2, 8, 4),
     Variant{4, 0, 0, launch_slab_rows, launch_slab_cols},
 };
 #undef VARIANT

@@ -124,12 +124,12 @@ __device__ __forceinline__ void team_dot(const int32_t *__restrict__ idx,
   for (int v = 0; v < kVW; ++v) hi[v] = lo[v] = 0.f;
   int64_t e = beg + sub;
   while (e < end) {
-    float acc[kU][kVW];
+    float acc[kVW];
 #pragma unroll
-    for (int u = 0; u < kU; ++u)
-#pragma unroll
-      for (int v = 0; v < kVW; ++v) acc[u][v] = 0.f;
+    for (int v = 0; v < kVW; ++v) acc[v] = 0.f;
     int steps = 0;
+    // kU entries per step: their indices and values first, then kU gathers in
+    // flight at once, then the multiply-adds
     for (; steps < kRun && e + (kU - 1) * S < end; ++steps, e += kU * S) {
       int32_t c[kU];
       float a[kU];
@@ -138,13 +138,13 @@ __device__ __forceinline__ void team_dot(const int32_t *__restrict__ idx,
         c[u] = __ldg(idx + e + u * S);
         a[u] = __ldg(val + e + u * S);
       }
+      float g[kU][kVW];
 #pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        float g[kVW];
-        VecF<kVW>::load(xq + (int64_t)c[u] * kp, g);
+      for (int u = 0; u < kU; ++u) VecF<kVW>::load(xq + (int64_t)c[u] * kp, g[u]);
 #pragma unroll
-        for (int v = 0; v < kVW; ++v) acc[u][v] = fmaf(a[u], g[v], acc[u][v]);
-      }
+      for (int u = 0; u < kU; ++u)
+#pragma unroll
+        for (int v = 0; v < kVW; ++v) acc[v] = fmaf(a[u], g[u][v], acc[v]);
     }
     if (steps < kRun) {  // the line's last few entries, one at a time
       for (; e < end; e += S) {
@@ -152,16 +152,11 @@ __device__ __forceinline__ void team_dot(const int32_t *__restrict__ idx,
         VecF<kVW>::load(xq + (int64_t)__ldg(idx + e) * kp, g);
         const float a = __ldg(val + e);
 #pragma unroll
-        for (int v = 0; v < kVW; ++v) acc[0][v] = fmaf(a, g[v], acc[0][v]);
+        for (int v = 0; v < kVW; ++v) acc[v] = fmaf(a, g[v], acc[v]);
       }
     }
 #pragma unroll
-    for (int v = 0; v < kVW; ++v) {
-      float r = acc[0][v];
-#pragma unroll
-      for (int u = 1; u < kU; ++u) r += acc[u][v];
-      two_sum_add(hi[v], lo[v], r);
-    }
+    for (int v = 0; v < kVW; ++v) two_sum_add(hi[v], lo[v], acc[v]);
   }
 #pragma unroll
   for (int v = 0; v < kVW; ++v) {

@@ -62,5 +62,5 @@ def test_variant_table(pkg):
             assert e.code == -1
             break
     assert len(seen) == 13 and len(set(seen)) == 13
-    assert all(vw in (2, 4) and lpr in (8, 16, 32) and u in (1, 2) for vw, lpr, u in seen[:12])
+    assert all(vw in (2, 4) and lpr in (8, 16, 32) and u in (2, 4) for vw, lpr, u in seen[:12])
     assert seen[12] == (4, 0, 0)  # the slab form

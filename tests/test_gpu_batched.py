@@ -144,7 +144,7 @@ def test_batch_arguments_are_checked(pkg, grid32):
             assert e.value.code == -1
         # a variant too narrow for the block: float2 gathers of 32 columns on
         # 8 lanes
-        narrow = [v for v in range(13) if pkg._native.batch_variant(v) == (2, 8, 1)]
+        narrow = [v for v in range(13) if pkg._native.batch_variant(v) == (2, 8, 2)]
         with pytest.raises(pkg._native.PlsqrError):
             ctx.batch_lsqr(np.zeros((32, prob.m_k)), variant_rows=narrow[0])
 
