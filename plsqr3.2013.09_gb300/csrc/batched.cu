@@ -301,11 +301,11 @@ static int batch_setup(plsqr_ctx *ctx) {
     CK(cudaMemsetAsync(B->cf, 0, sizeof(BatchCoef), ctx->stream));
     const std::vector<double> ones(kBatchMax, 1.0);
     CK(cudaMemcpy(B->LAM, ones.data(), sizeof(double) * kBatchMax, cudaMemcpyHostToDevice));
-    // grids: four resident blocks of 256 threads per SM for the products
-    // (their launch bounds), one block per SM on the damping rows
-    B->gk = 4 * ctx->sm_count;
+    // grids: kTeamBlocksPerSm resident blocks of 256 threads per SM for the
+    // team products (their launch bounds), one block per SM on the damping rows
+    B->gk = kTeamBlocksPerSm * ctx->sm_count;
     B->gd = ctx->sm_count;
-    B->gc = 4 * ctx->sm_count;
+    B->gc = kTeamBlocksPerSm * ctx->sm_count;
     B->gres = 8 * ctx->sm_count;
     B->gvec = 8 * ctx->sm_count;
     std::vector<int64_t> kr((size_t)ctx->m_k + 1), kc((size_t)ctx->n + 1), dc((size_t)ctx->n + 1);

@@ -31,6 +31,10 @@ namespace plsqr {
 
 constexpr int kBatchMax = 32;
 constexpr int kBatchThreads = 256;
+// resident blocks per SM of the team products (their launch bounds): five
+// measured faster than four (more gathers in flight) despite a few spilled
+// registers
+constexpr int kTeamBlocksPerSm = 5;
 
 // Per-right-hand-side coefficients handed from one kernel to the next.
 struct BatchCoef {
@@ -212,7 +216,7 @@ __device__ __forceinline__ void rows_finish(const double *parts, int n_parts, in
 // 32/kp rows per warp with one lane per right-hand side, in FP64.  The last
 // block forms beta_j = ||u_j|| and, in LSQR mode, anorm (source/lsqr.c:526-528).
 template <int kVW, int kLPR, int kU>
-__global__ void __launch_bounds__(kBatchThreads, 4)
+__global__ void __launch_bounds__(kBatchThreads, kTeamBlocksPerSm)
     k_bprod_rows(CsrT<float> K, Csr D, const int32_t *__restrict__ wpart, int gk, int kp, int k,
                  const float *__restrict__ vf, const double *__restrict__ v64,
                  double *__restrict__ u, const double *__restrict__ lambda, int mode,
@@ -342,7 +346,7 @@ __device__ __forceinline__ void cols_finish(const double *parts, int n_parts, in
 // its sums.  The last block forms alpha_j and the rotation of the iteration
 // (source/lsqr.c:551-636), or the start-up values (source/lsqr.c:387-409).
 template <int kVW, int kLPR, int kU>
-__global__ void __launch_bounds__(kBatchThreads, 4)
+__global__ void __launch_bounds__(kBatchThreads, kTeamBlocksPerSm)
     k_bprod_cols(CsrT<float> KC, Csr DC, const int32_t *__restrict__ wpart, int kp, int k,
                  const float *__restrict__ uf, const double *__restrict__ u64, int m_k,
                  double *__restrict__ v, const double *__restrict__ lambda, int mode,

@@ -13,7 +13,7 @@
 // and returns; the other blocks see the word at their next wait, so the
 // launch always ends.
 //
-// Per iteration (four barriers):
+// Per iteration (four barriers; three in the default mode, see solve_one):
 //   A  u = -alpha u + A v            kernel rows (a warp's range, a row per
 //                                    lane), damping rows by thread
 //   B  beta = ||u||, u /= beta       every block sums the group's partials
@@ -296,19 +296,26 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
   if (!group_sync(g)) return false;
   const int iters = sh.S.done ? 0 : P.iters;
 
+  // Default mode: u is kept unscaled between B and the next A, so B needs no
+  // pass over u and no barrier of its own: C multiplies its column sums by
+  // 1/beta and A scales each u element as it reads it (the same product the
+  // reference's scaling rounds).  rb_u: the scale u still carries.
+  double rb_u = 1.0;
   for (int it = 0; it < iters; ++it) {
     // A: u = -alpha u + A v
     const double s1 = -sh.S.alpha;
     sq = 0.0;
     for (int r = P.kpart[gw] + lane; r < P.kpart[gw + 1]; r += 32) {
-      const double y = plsqr::dadd(plsqr::dmul(s1, ld(u + r)), kernel_row<kExact>(P, v, r));
+      const double ur = kExact ? ld(u + r) : plsqr::dmul(ld(u + r), rb_u);
+      const double y = plsqr::dadd(plsqr::dmul(s1, ur), kernel_row<kExact>(P, v, r));
       u[r] = y;
       sq = fma(y, y, sq);
     }
     for (int64_t r = gt; r < P.m_d; r += gstride) {
       const double t = seq_line<kExact>(P.dr_idx, P.dr_val, v, P.dr_ptr[r], P.dr_ptr[r + 1]);  // CPUSpMV.c:67-70
       double *p = u + P.m_k + r;
-      const double y = plsqr::dadd(plsqr::dmul(s1, ld(p)), t);
+      const double ur = kExact ? ld(p) : plsqr::dmul(ld(p), rb_u);
+      const double y = plsqr::dadd(plsqr::dmul(s1, ur), t);
       *p = y;
       sq = fma(y, y, sq);
     }
@@ -328,15 +335,21 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
       sh.rb = beta > 0.0 ? plsqr::ddiv(1.0, beta) : 0.0;
     }
     __syncthreads();
-    if (sh.rb != 0.0)
-      for (int64_t i = gt; i < m; i += gstride) u[i] = plsqr::dmul(ld(u + i), sh.rb);
-    if (!group_sync(g)) return false;
+    if (kExact) {
+      if (sh.rb != 0.0)
+        for (int64_t i = gt; i < m; i += gstride) u[i] = plsqr::dmul(ld(u + i), sh.rb);
+      if (!group_sync(g)) return false;
+    } else {
+      rb_u = sh.rb != 0.0 ? sh.rb : 1.0;  // beta = 0: u is left as it is
+    }
     // C: v = -beta v + A^T u (skipped when beta = 0, source/lsqr.c:530)
     sq = 0.0;
     if (sh.S.s_beta_pos) {
       const double s2 = -sh.S.beta;
+      const double rb = sh.rb;
       for (int c = P.cpart[gw] + lane; c < P.cpart[gw + 1]; c += 32) {
-        const double t = plsqr::dadd(kernel_col<kExact>(P, u, c), damp_col<kExact>(P, u, c));
+        double t = plsqr::dadd(kernel_col<kExact>(P, u, c), damp_col<kExact>(P, u, c));
+        if (!kExact) t = plsqr::dmul(t, rb);
         const double y = plsqr::dadd(plsqr::dmul(s2, ld(v + c)), t);
         v[c] = y;
         sq = fma(y, y, sq);
