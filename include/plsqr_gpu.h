@@ -110,7 +110,8 @@ typedef struct {
                              like result.txt (source/lsqr.c:246-268, 780-905) */
   /* PLSQR_PREC_MIXED contexts only: `sweeps` outer refinement steps, each
    * an FP32 LSQR of `inner` iterations on r = b - A x (FP64); the history
-   * then holds sweeps * inner + 1 records and lsqr_iteration is unused.     */
+   * then holds sweeps * inner + 1 records and lsqr_iteration is unused.
+   * damp > 0 requires sweeps = 1 (PLSQR_ERR_ARG otherwise).                 */
   int32_t sweeps, inner;
 } plsqr_lsqr_args;
 
@@ -246,7 +247,8 @@ typedef struct {
                             -1 = pick by timing (cached per operator shape)  */
   int32_t variant_cols;  /* the same for A^T y                                */
   int32_t pad;
-  double damp, atol, btol, conlim; /* lsqr() arguments of every solve         */
+  double damp, atol, btol, conlim; /* lsqr() arguments of every solve; damp > 0
+                                      requires sweeps = 1                    */
   const double *b_k;     /* [k][m_k]: right-hand side j at b_k + j*m_k        */
   const double *lambda;  /* [k] damping-row weights; NULL = all 1             */
   const double *x_ref;   /* [k][n] solutions to measure the error against

@@ -500,6 +500,12 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
                                 plsqr_iter *hist, plsqr_result *res, plsqr_batch_info *info) {
   if (!ctx || !a || !a->b_k) return PLSQR_ERR_ARG;
   if (a->k < 1 || a->k > kBatchMax || a->sweeps < 1 || a->inner < 1) return PLSQR_ERR_ARG;
+  // as in the mixed solver: a damped sweep regularises the correction, not
+  // the solution, so damp > 0 allows one sweep only
+  if (a->damp != 0.0 && a->sweeps > 1) {
+    ctx_set_error(ctx, "damp > 0 needs sweeps = 1");
+    return PLSQR_ERR_ARG;
+  }
   const int k = a->k, kw = width_for(k);
   if ((a->variant_rows >= 0 && !variant_ok(a->variant_rows, kw)) ||
       (a->variant_cols >= 0 && !variant_ok(a->variant_cols, kw)) ||

@@ -224,6 +224,14 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   (void)w;
   (void)se;
   if (args->sweeps < 1 || args->inner < 1 || args->want_se) return PLSQR_ERR_ARG;
+  // A sweep solves for the correction dx with damp^2 ||dx||^2, not
+  // damp^2 ||x + dx||^2, so damped refinement past the first sweep would
+  // solve another problem: refuse it.
+  if (args->damp != 0.0 && args->sweeps > 1) {
+    ctx_set_error(ctx, "damp > 0 needs sweeps = 1 (refinement sweeps would regularise the "
+                       "correction instead of the solution)");
+    return PLSQR_ERR_ARG;
+  }
   int rc;
   if ((rc = mixed_prepare(ctx))) return rc;
   MixedState *M = ctx->mixed;

@@ -137,7 +137,8 @@ def test_batch_arguments_are_checked(pkg, grid32):
         for bad in (dict(b_k=np.zeros((33, prob.m_k))), dict(b_k=np.zeros((2, prob.m_k)),
                                                             sweeps=0),
                     dict(b_k=np.zeros((2, prob.m_k)), variant_rows=99),
-                    dict(b_k=np.zeros((2, prob.m_k)), lam=[1.0, -1.0])):
+                    dict(b_k=np.zeros((2, prob.m_k)), lam=[1.0, -1.0]),
+                    dict(b_k=np.zeros((2, prob.m_k)), damp=0.1, sweeps=2)):
             b = bad.pop("b_k")
             with pytest.raises(pkg._native.PlsqrError) as e:
                 ctx.batch_lsqr(b, **bad)

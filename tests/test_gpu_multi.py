@@ -95,3 +95,15 @@ def test_bounded_wait_returns_timeout(pkg, uneven):
         assert all(r["itn"] == 5 for r in out["results"])
         with pytest.raises(pkg._native.PlsqrError):
             mp.set_wait(10)
+
+
+def test_damped_problems_match_one_problem_path(pkg, uneven):
+    """lsqr()'s damp (source/lsqr.c:515-523 rotation) in the persistent launch."""
+    probs = uneven[:2]
+    with pkg.multi.Multi(probs, damp=0.05) as mp:
+        out = mp.solve()
+    for p, x, h in zip(probs, out["x"], out["hist"]):
+        with pkg.Context(p) as c:
+            ref = c.lsqr(lsqr_iteration=p.iterations, damp=0.05)
+        assert rel(x, ref["x"]) <= 1e-10
+        assert np.allclose(h["rnorm"], ref["hist"]["rnorm"], rtol=1e-10, atol=0)

@@ -226,3 +226,15 @@ def test_mixed_precision_reaches_1e6_of_fp64_solution(pkg, problems):
     assert err[0] == 1.0
     assert rel(out["x"], xstar) <= 1e-6
     assert abs(err[-1] - rel(out["x"], xstar)) <= 1e-3 * err[-1] + 1e-12
+
+
+def test_mixed_precision_refuses_damped_refinement(pkg, problems):
+    """A refinement sweep regularises the correction, not the solution, so a
+    damped solve allows one sweep only."""
+    prob = problems("grid32")
+    with pkg.Context(prob, precision="mixed") as cm:
+        with pytest.raises(pkg._native.PlsqrError) as e:
+            cm.lsqr(damp=0.1, sweeps=2, inner=10)
+        assert e.value.code == -1
+        out = cm.lsqr(damp=0.1, sweeps=1, inner=10)
+        assert np.all(np.isfinite(out["x"]))
