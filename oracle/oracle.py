@@ -53,6 +53,18 @@ def build(with_reference: bool = False) -> None:
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", "-j8"], check=True)
 
 
+REF_GPU_APROD_BIN = HERE / "_ref" / "PLSQR3_gpu_aprod"
+
+
+def build_gpu_aprod():
+    """The reference program linked with the GPU operator shim (make
+    ref_gpu_aprod), where the reference tree is mounted; its path, or None."""
+    if not (Path("/root/reference/source/lsqr.c").exists() and shutil.which("gcc")):
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref_gpu_aprod", "-j8"], check=True)
+    return REF_GPU_APROD_BIN
+
+
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
