@@ -253,6 +253,11 @@ typedef struct {
   const double *lambda;  /* [k] damping-row weights; NULL = all 1             */
   const double *x_ref;   /* [k][n] solutions to measure the error against
                             (history field err), or NULL                      */
+  const double *x0;      /* [k][n] starting solutions (warm start), or NULL =
+                            0: the first sweep corrects from b - A x0.  A
+                            right-hand side whose starting residual is not
+                            below ||b|| starts from 0 instead (cold start);
+                            info.warm says which kept x0.  Needs damp = 0.   */
 } plsqr_batch_args;
 void plsqr_default_batch_args(plsqr_batch_args *a);
 
@@ -267,7 +272,7 @@ typedef struct {
   int32_t k, kp;                    /* right-hand sides, padded block width   */
   int32_t variant_rows, variant_cols; /* variants in use                      */
   int32_t tuned;                    /* 1: timed by the last call, 0: cached   */
-  int32_t pad;
+  int32_t warm;                     /* bit j: right-hand side j kept its x0   */
   double ms_rows, ms_cols;          /* their times per product when timed     */
 } plsqr_batch_info;
 

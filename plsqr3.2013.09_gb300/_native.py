@@ -73,12 +73,13 @@ class SynthParams(C.Structure):
 class BatchArgs(C.Structure):
     _fields_ = [("k", i32), ("sweeps", i32), ("inner", i32), ("variant_rows", i32),
                 ("variant_cols", i32), ("pad", i32), ("damp", f64), ("atol", f64),
-                ("btol", f64), ("conlim", f64), ("b_k", vp), ("lambda_", vp), ("x_ref", vp)]
+                ("btol", f64), ("conlim", f64), ("b_k", vp), ("lambda_", vp), ("x_ref", vp),
+                ("x0", vp)]
 
 
 class BatchInfo(C.Structure):
     _fields_ = [("k", i32), ("kp", i32), ("variant_rows", i32), ("variant_cols", i32),
-                ("tuned", i32), ("pad", i32), ("ms_rows", f64), ("ms_cols", f64)]
+                ("tuned", i32), ("warm", i32), ("ms_rows", f64), ("ms_cols", f64)]
 
 
 class ProblemDesc(C.Structure):

@@ -461,6 +461,15 @@ static int ensure_graph(plsqr_ctx *ctx, BatchState *B) {
   return PLSQR_OK;
 }
 
+// X[:, j] = 0 for the right-hand sides j whose bit is set in `mask`.
+static __global__ void k_bzero_cols(double *__restrict__ x, int64_t rows, int kw,
+                                    unsigned int mask) {
+  const int64_t total = rows * kw;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if ((mask >> (i % kw)) & 1u) x[i] = 0.0;
+}
+
 // ---- C ABI ----------------------------------------------------------------------
 extern "C" void plsqr_default_batch_args(plsqr_batch_args *a) {
   if (!a) return;
@@ -502,8 +511,8 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
   if (a->k < 1 || a->k > kBatchMax || a->sweeps < 1 || a->inner < 1) return PLSQR_ERR_ARG;
   // as in the mixed solver: a damped sweep regularises the correction, not
   // the solution, so damp > 0 allows one sweep only
-  if (a->damp != 0.0 && a->sweeps > 1) {
-    ctx_set_error(ctx, "damp > 0 needs sweeps = 1");
+  if (a->damp != 0.0 && (a->sweeps > 1 || a->x0)) {
+    ctx_set_error(ctx, "damp > 0 needs sweeps = 1 and no starting solution");
     return PLSQR_ERR_ARG;
   }
   const int k = a->k, kw = width_for(k);
@@ -545,7 +554,32 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
     k_bgather<<<gl, 256, 0, s>>>(B->stage, n, n, kw, k, B->XR);
   }
   CK(cudaGetLastError());
-  CK(cudaMemsetAsync(B->X, 0, sizeof(double) * n * kw, s));
+  // starting solutions; the warm-start test needs ||b_j|| and, for the
+  // history, ||x0_j - xref_j|| / ||xref_j||
+  std::vector<double> bnorm((size_t)k, 0.0), err0((size_t)k, 1.0);
+  unsigned int warm = 0;
+  if (a->x0) {
+    CK(cudaMemcpyAsync(B->stage, a->x0, sizeof(double) * n * k, cudaMemcpyHostToDevice, s));
+    k_bgather<<<gl, 256, 0, s>>>(B->stage, n, n, kw, k, B->X);
+    CK(cudaGetLastError());
+    for (int j = 0; j < k; ++j) {
+      double sb = 0.0;
+      for (int64_t r = 0; r < mk; ++r) sb += a->b_k[(int64_t)j * mk + r] * a->b_k[(int64_t)j * mk + r];
+      bnorm[(size_t)j] = sqrt(sb);
+      if (a->x_ref) {
+        double d2 = 0.0, r2 = 0.0;
+        for (int64_t c = 0; c < n; ++c) {
+          const double xr = a->x_ref[(int64_t)j * n + c], d = a->x0[(int64_t)j * n + c] - xr;
+          d2 += d * d;
+          r2 += xr * xr;
+        }
+        err0[(size_t)j] = r2 > 0.0 ? sqrt(d2 / r2) : 0.0;
+      }
+    }
+    warm = k >= 32 ? 0xffffffffu : ((1u << k) - 1u);
+  } else {
+    CK(cudaMemsetAsync(B->X, 0, sizeof(double) * n * kw, s));
+  }
   // history: [k][total + 1]
   B->hist_stride = (int)(total + 1);
   if (B->hist_cap < (int64_t)k * (total + 1)) {
@@ -564,6 +598,7 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
   int last_itn = 0;
   CK(cudaEventRecord(ctx->ev0, s));
   for (int sw = 0; sw < S; ++sw) {
+   for (int attempt = 0; attempt < 2; ++attempt) {
     std::vector<DevState> h((size_t)k);
     memset(h.data(), 0, sizeof(DevState) * k);
     for (int j = 0; j < k; ++j) {
@@ -592,6 +627,22 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * k, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (sw == 0 && attempt == 0 && a->x0) {
+      // cold start where x0 does not lower the residual: ||[b; 0] - A x0|| >= ||b||
+      unsigned int cold = 0;
+      for (int j = 0; j < k; ++j)
+        if (!(cur[(size_t)j].beta < bnorm[(size_t)j])) cold |= 1u << j;
+      if (cold) {
+        warm &= ~cold;
+        for (int j = 0; j < k; ++j)
+          if ((cold >> j) & 1u) err0[(size_t)j] = 1.0;
+        k_bzero_cols<<<gl, 256, 0, s>>>(B->X, n, kw, cold);
+        CK(cudaGetLastError());
+        continue;  // the start-up again, from the new X
+      }
+    }
+    break;
+   }
     bool all_done = true;
     for (int j = 0; j < k; ++j) {
       const DevState &c = cur[(size_t)j];
@@ -604,7 +655,7 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
         e.arnorm = c.arnorm;
         e.test1 = 1.0;
         e.test2 = c.beta > 0.0 ? c.alpha / c.beta : 0.0;
-        e.err = B->has_ref ? 1.0 : -1.0;
+        e.err = B->has_ref ? err0[(size_t)j] : -1.0;
       }
     }
     if (all_done) break;  // A^T r_j = 0 for every j: X solves every problem
@@ -651,6 +702,7 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
     }
   }
   fill_info(B, info);
+  if (info) info->warm = (int32_t)warm;
   return PLSQR_OK;
 }
 

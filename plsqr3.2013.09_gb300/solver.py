@@ -161,7 +161,7 @@ class Context:
         return dict(x=x, w=w, se=se, hist=hist, result=res)
 
     # -- several right-hand sides ----------------------------------------------
-    def batch_lsqr(self, b_k, *, lam=None, x_ref=None, sweeps: int = 4, inner: int = 50,
+    def batch_lsqr(self, b_k, *, lam=None, x_ref=None, x0=None, sweeps: int = 4, inner: int = 50,
                    damp: float = 0.0, atol: float = 1e-10, btol: float = 1e-10,
                    conlim: float = 100.0, variant_rows: int = -1,
                    variant_cols: int = -1) -> dict:
@@ -169,7 +169,9 @@ class Context:
 
         b_k: (k, m_k) right-hand sides; lam: (k,) damping-row weights (solve j
         uses [K; lam_j D]); x_ref: (k, n) solutions for the history's err
-        field.  Returns x (k, n), hist (k, sweeps*inner + 1), per-solve
+        field; x0: (k, n) starting solutions (warm start, with the cold start
+        as fallback where b - A x0 is not smaller than b; info["warm"] has bit
+        j set where x0 was kept).  Returns x (k, n), hist (k, sweeps*inner + 1), per-solve
         results and the product variants used."""
         b = np.ascontiguousarray(b_k, np.float64)
         if b.ndim != 2 or b.shape[1] != self.m_k:
@@ -181,12 +183,15 @@ class Context:
         xr = None if x_ref is None else np.ascontiguousarray(x_ref, np.float64)
         if xr is not None and xr.shape != (k, self.n):
             raise ValueError(f"x_ref must have shape ({k}, {self.n})")
+        xs = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+        if xs is not None and xs.shape != (k, self.n):
+            raise ValueError(f"x0 must have shape ({k}, {self.n})")
         a = N.BatchArgs()
         N.lib().plsqr_default_batch_args(C.byref(a))
         a.k, a.sweeps, a.inner = k, sweeps, inner
         a.variant_rows, a.variant_cols = variant_rows, variant_cols
         a.damp, a.atol, a.btol, a.conlim = damp, atol, btol, conlim
-        a.b_k, a.lambda_, a.x_ref = N.ptr(b), N.ptr(lm), N.ptr(xr)
+        a.b_k, a.lambda_, a.x_ref, a.x0 = N.ptr(b), N.ptr(lm), N.ptr(xr), N.ptr(xs)
         x = np.empty((k, self.n))
         hist = np.zeros((k, sweeps * inner + 1), N.ITER_DTYPE)
         res = (N.Result * k)()
@@ -196,7 +201,7 @@ class Context:
                     "plsqr_batch_lsqr")
         results = [{f: getattr(r, f) for f, _ in N.Result._fields_ if f != "pad"} for r in res]
         return dict(x=x, hist=hist, results=results,
-                    info={f: getattr(info, f) for f, _ in N.BatchInfo._fields_ if f != "pad"})
+                    info={f: getattr(info, f) for f, _ in N.BatchInfo._fields_})
 
     def batch_bench_aprod(self, k: int, mode: int, variant: int = -1, reps: int = 5) -> float:
         """ms per launch of the k-wide product (mode 1 or 2) of a variant

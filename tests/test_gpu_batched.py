@@ -160,3 +160,32 @@ def test_damping_weight_round_trip(pkg, problems):
         back = c.lsqr(lsqr_iteration=20)
     assert np.array_equal(ref["x"], back["x"])
     assert not np.array_equal(ref["x"], w3["x"])
+
+
+def test_warm_start_and_cold_fallback(pkg, grid32):
+    """x0 near the solution is kept and saves iterations; an x0 that does not
+    lower the residual falls back to the cold start, bit for bit."""
+    prob, insts = grid32
+    sel = [insts[0], insts[24]]
+    b = np.stack([i.b_k for i in sel])
+    xstar = np.stack([fp64_solution(pkg, prob, i, 800)["x"] for i in sel])
+    rng = np.random.default_rng(5)
+    near = xstar * (1.0 + 0.01 * rng.standard_normal(xstar.shape))
+    far = 100.0 * rng.standard_normal(xstar.shape)
+    kw = dict(x_ref=xstar, sweeps=3, inner=60, variant_rows=1, variant_cols=1)
+    with pkg.Context(prob) as ctx:
+        cold = ctx.batch_lsqr(b, **kw)
+        warm = ctx.batch_lsqr(b, x0=near, **kw)
+        back = ctx.batch_lsqr(b, x0=np.stack([near[0], far[1]]), **kw)
+    assert cold["info"]["warm"] == 0 and warm["info"]["warm"] == 0b11
+    assert back["info"]["warm"] == 0b01
+    for j in range(2):
+        e_cold, e_warm = cold["hist"]["err"][j], warm["hist"]["err"][j]
+        assert e_warm[0] == pytest.approx(rel(near[j], xstar[j]), rel=1e-12)
+        assert rel(warm["x"][j], xstar[j]) <= 1e-6
+        k_cold = int(np.argmax(e_cold <= 1e-6))
+        k_warm = int(np.argmax(e_warm <= 1e-6))
+        assert e_warm[k_warm] <= 1e-6 and k_warm < k_cold
+    # the far start fell back: the same bits as the cold solve
+    assert np.array_equal(back["x"][1], cold["x"][1])
+    assert np.array_equal(back["x"][0], warm["x"][0])
