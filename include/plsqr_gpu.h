@@ -346,6 +346,34 @@ int plsqr_multi_plan_host(const double *bytes, const int32_t *iters, int32_t cou
  * given limit: returns PLSQR_ERR_TIMEOUT and leaves the context usable. */
 int plsqr_multi_check_wait(plsqr_multi *mp, int64_t wait_ns);
 
+/* ---- learned warm start ---------------------------------------------------
+ * No counterpart in the reference.  A 3-D U-Net (3 levels, 16/32/64
+ * channels, BF16 weights with FP32 masters, FP32 accumulation) on the model
+ * grid maps the column-norm-scaled back-projection A^T b to a starting
+ * solution x0, which plsqr_batch_args.x0 hands to the solver (with the cold
+ * start as fallback).  Volumes are nx*ny*nz floats in column order
+ * ((z*ny + y)*nx + x); nx, ny, nz multiples of 4. */
+typedef struct plsqr_unet plsqr_unet;
+int plsqr_unet_create(int32_t nx, int32_t ny, int32_t nz, uint64_t seed, int32_t device,
+                      plsqr_unet **out);
+void plsqr_unet_destroy(plsqr_unet *net);
+const char *plsqr_unet_last_error(const plsqr_unet *net);
+/* x0 = net(in) (host arrays). */
+int plsqr_unet_predict(plsqr_unet *net, const float *in, float *out);
+/* One Adam step on the squared error against target (host arrays); *loss is
+ * the mean squared error in units of the input's root mean square. */
+int plsqr_unet_train_step(plsqr_unet *net, const float *in, const float *target, float lr,
+                          float *loss);
+/* All weights (set = 0: read into buf; 1: load from buf).  buf = NULL:
+ * *count = the number of floats. */
+int plsqr_unet_weights(plsqr_unet *net, float *buf, int64_t *count, int32_t set);
+/* One 3x3x3 convolution + ReLU layer, forward and backward, on host arrays
+ * (x [n][cin], w [cout][27*cin] with tap-major k, dy [n][cout]); the
+ * network's kernels checked in isolation. */
+int plsqr_nn_conv3d_check(int32_t nx, int32_t ny, int32_t nz, int32_t cin, int32_t cout,
+                          const float *x, const float *w, const float *b, const float *dy,
+                          float *y, float *dx, float *dw, float *db);
+
 /* Weight the context's damping rows: D becomes lambda * D (both copies, from
  * the values the context was created with).  For one-right-hand-side solves
  * of the weighted problems above. */

@@ -8,7 +8,7 @@ operator/driver interface (solver.Context).
 The directory name is not a valid Python identifier; load it with
 __graft_entry__.load_package(), which registers it as ``plsqr_gb300``.
 """
-from . import _native, synth, solver, batch, multi  # noqa: F401
+from . import _native, synth, solver, batch, multi, warm  # noqa: F401
 from .solver import Context  # noqa: F401
 from .synth import CONFIGS, Problem, generate, read_files, write_files  # noqa: F401
 

@@ -129,6 +129,13 @@ SIGNATURES = {
     "plsqr_batch_lsqr": (C.c_int, [vp, C.POINTER(BatchArgs), vp, vp, vp, C.POINTER(BatchInfo)]),
     "plsqr_batch_bench_aprod": (C.c_int, [vp, i32, C.c_int, i32, C.c_int, C.POINTER(f64)]),
     "plsqr_set_damping_weight": (C.c_int, [vp, f64]),
+    "plsqr_unet_create": (C.c_int, [i32, i32, i32, u64, i32, C.POINTER(vp)]),
+    "plsqr_unet_destroy": (None, [vp]),
+    "plsqr_unet_last_error": (C.c_char_p, [vp]),
+    "plsqr_unet_predict": (C.c_int, [vp, vp, vp]),
+    "plsqr_unet_train_step": (C.c_int, [vp, vp, vp, C.c_float, C.POINTER(C.c_float)]),
+    "plsqr_unet_weights": (C.c_int, [vp, vp, C.POINTER(i64), i32]),
+    "plsqr_nn_conv3d_check": (C.c_int, [i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
     "plsqr_default_problem": (None, [C.POINTER(ProblemDesc)]),
     "plsqr_multi_create": (C.c_int, [C.POINTER(ProblemDesc), i32, C.POINTER(Opts), C.POINTER(vp)]),
     "plsqr_multi_destroy": (None, [vp]),

@@ -23,7 +23,7 @@ LIB = PKG / "lib"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["plsqr_gpu.cu", "mixed.cu", "slab.cu", "noalloc.cu", "batched.cu", "multi.cu"]
+CU_SOURCES = ["plsqr_gpu.cu", "mixed.cu", "slab.cu", "noalloc.cu", "batched.cu", "multi.cu", "unet.cu"]
 CPP_SOURCES = ["formats.cpp", "synth.cpp", "report.cpp", "files_ctx.cpp"]
 LIBNAME = "libplsqr_gpu.so"
 
