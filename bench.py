@@ -172,7 +172,12 @@ def main() -> int:
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: build the context, run one short solve, exit")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--extension", default=None, choices=["batched", "uneven"],
+    ap.add_argument("--train", type=int, default=2000, help="warm start: training pairs")
+    ap.add_argument("--epochs", type=int, default=2, help="warm start: passes over the pairs")
+    ap.add_argument("--heldout", type=int, default=200, help="warm start: held-out seeds")
+    ap.add_argument("--timed", type=int, default=16,
+                    help="warm start: held-out seeds timed to 1e-6 against FP64 references")
+    ap.add_argument("--extension", default=None, choices=["batched", "uneven", "warm"],
                     help="measure an extension instead: 32 right-hand sides on the "
                          "96x96x32 operator, or the 24 uneven problems in one launch")
     ap.add_argument("--variant-rows", type=int, default=-1,
@@ -186,7 +191,7 @@ def main() -> int:
     if args.extension and not args.profile:
         if rank != 0:
             return 0
-        fn = bench_batched if args.extension == "batched" else bench_uneven
+        fn = {"batched": bench_batched, "uneven": bench_uneven, "warm": bench_warm}[args.extension]
         print(json.dumps(fn(pkg, args, local)))
         return 0
     cfg = pkg.CONFIGS[args.config]
@@ -499,6 +504,102 @@ def bench_uneven(pkg, args, device) -> dict:
             "sequential_seconds": seq, "speedup_vs_sequential": seq / min(t),
             "problem_iterations_per_s": its / min(t),
             "max_rel_diff_vs_one_problem_path": worst}
+
+
+def bench_warm(pkg, args, device) -> dict:
+    """Learned warm start on the 96x96x32 geometry: train the U-Net on
+    (column-norm-scaled A^T b, x_LSQR) pairs of seeded models, then compare,
+    on held-out seeds, the iterations and time to 1e-6 of each one's FP64
+    solution for plain FP64 LSQR (cold), mixed precision (cold) and mixed
+    precision from the network's x0 (warm, cold start as fallback)."""
+    tol = 1e-6
+    name = args.config
+    iters = args.iterations or pkg.CONFIGS[name]["iterations"]
+    W = pkg.warm
+    t_all = time.perf_counter()
+    prob = pkg.generate(name)
+    grid = prob.meta["grid"]
+    ctx = pkg.Context(prob, device=device)
+    cn2 = W.column_norms2(prob)
+    seeds_train = list(range(args.train))
+    seeds_test = list(range(1_000_000, 1_000_000 + args.heldout))
+
+    def inputs(seeds):
+        zs, bs, xt = [], [], []
+        for s in seeds:
+            x_true, b = W.measurements(ctx, name, grid, s)
+            bs.append(b)
+            xt.append(x_true)
+            zs.append(W.back_projection(ctx, b, cn2))
+        return zs, bs, xt
+
+    t0 = time.perf_counter()
+    z_tr, b_tr, _ = inputs(seeds_train)
+    x_tr, _, _ = W.solve_batches(ctx, b_tr, iters)
+    t_data = time.perf_counter() - t0
+    log(f"training pairs: {len(x_tr)} in {t_data:.1f}s")
+    # one global factor brings the solutions to the inputs' scale (the
+    # network itself divides its input by, and multiplies its output with,
+    # the input's root mean square)
+    rms = lambda v: float(np.sqrt(np.mean(v * v)))
+    c = float(np.median([rms(x) / max(rms(z), 1e-300) for x, z in zip(x_tr, z_tr)]))
+    losses = []
+    t0 = time.perf_counter()
+    with W.UNet(grid, seed=1, device=device) as net:
+        for ep in range(args.epochs):
+            lr = 1e-3 if ep == 0 else 3e-4
+            order = np.random.default_rng(ep).permutation(len(z_tr))
+            for i in order:
+                losses.append(net.train_step(z_tr[i], x_tr[i] / c, lr))
+            log(f"epoch {ep}: mean loss {np.mean(losses[-len(order):]):.4f}")
+        t_train = time.perf_counter() - t0
+        z_te, b_te, _ = inputs(seeds_test)
+        x_te, _, _ = W.solve_batches(ctx, b_te, iters)
+        x0_te = [c * net.predict(z) for z in z_te]
+    pred_err = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(x0_te, x_te)]
+    # timed subset: FP64 reference solutions (twice the iterations), then cold
+    # and warm tracked runs
+    nt = min(args.timed, len(seeds_test))
+    xstar, k64 = [], []
+    for j in range(nt):
+        xs = ctx.lsqr(b_te[j], lsqr_iteration=2 * iters)["x"]
+        ctx.set_reference_x(xs)
+        h = ctx.lsqr(b_te[j], lsqr_iteration=2 * iters)["hist"]
+        ctx.set_reference_x(None)
+        xstar.append(xs)
+        k64.append(first_below(h["err"], tol))
+    ms_fp64 = ctx.bench_iteration(reps=20)
+    inner = 2 * iters
+    _, h_cold, s_cold = W.solve_batches(ctx, b_te[:nt], inner, x_refs=xstar)
+    _, h_warm, s_warm = W.solve_batches(ctx, b_te[:nt], inner, x0s=x0_te[:nt], x_refs=xstar)
+    k_cold = [first_below(h["err"], tol) for h in h_cold]
+    k_warm = [first_below(h["err"], tol) for h in h_warm]
+    ok = [a is not None and b is not None and c is not None for a, b, c in zip(k64, k_cold, k_warm)]
+    sel = [j for j in range(nt) if ok[j]]
+    out = {"metric": "iterations to 1e-6 rel. error (vs FP64 solution), held-out seeds: "
+                     "FP64 cold / mixed cold / mixed from the learned warm start",
+           "unit": "iterations", "extension": "warm", "higher_is_better": False, "n_gpus": 1,
+           "dtype": "bf16 network, f32 products / f64 vectors",
+           "data": "synthetic (seeded models: 16-128 blobs + checkerboard, 1% noise)",
+           "config": {"workload": f"{name} geometry, U-Net 16/32/64 channels",
+                      "train_pairs": len(x_tr), "epochs": args.epochs,
+                      "heldout": len(seeds_test), "timed": nt},
+           "train_seconds": t_train, "data_seconds": t_data, "target_scale": c,
+           "loss_first_last": [float(np.mean(losses[:50])), float(np.mean(losses[-50:]))],
+           "x0_rel_err_vs_x_lsqr": {"median": float(np.median(pred_err)),
+                                    "p90": float(np.percentile(pred_err, 90))},
+           "per_instance": [{"fp64": k64[j], "mixed_cold": k_cold[j], "mixed_warm": k_warm[j]}
+                            for j in range(nt)],
+           "fp64_iteration_ms": ms_fp64,
+           "seconds_total": time.perf_counter() - t_all}
+    if sel:
+        m64 = float(np.mean([k64[j] for j in sel]))
+        mc = float(np.mean([k_cold[j] for j in sel]))
+        mw = float(np.mean([k_warm[j] for j in sel]))
+        out.update(value=mw, mean_iterations={"fp64": m64, "mixed_cold": mc, "mixed_warm": mw},
+                   warm_over_cold_iterations=mc / mw)
+    ctx.close()
+    return out
 
 
 if __name__ == "__main__":

@@ -3,9 +3,9 @@ back-projection A^T b to a starting solution x0 (plsqr_unet_*), trained on
 (A^T b, x_LSQR) pairs that this library's solvers produce, and handed to the
 batched solver as x0 (with the cold start as fallback).
 
-The model class: seeded x_true of 16-128 Gaussian blobs plus a checkerboard of
-random period (4-16 cells, amplitude 0-0.2), measured through the problem's
-kernel with 1% noise.
+The model class (model_instance): seeded x_true of 16-128 Gaussian blobs
+plus a checkerboard of random period (4-16 cells, amplitude 0-0.2), measured
+through the problem's kernel with 1% noise.
 """
 from __future__ import annotations
 
@@ -15,7 +15,6 @@ import numpy as np
 
 from . import _native as N
 from .batch import kernel_product, noisy
-from .synth import params
 
 
 class UNet:
@@ -98,10 +97,15 @@ def column_norms2(prob) -> np.ndarray:
     """||A e_c||^2 for every column c (kernel and damping parts)."""
     out = np.zeros(prob.n)
     for L in (prob.k_csc, prob.d_csc):
-        if L.nnz == 0:
-            continue
-        starts = np.minimum(L.ptr[:-1], L.nnz - 1)
-        out += np.add.reduceat(L.val * L.val, starts) * (np.diff(L.ptr) > 0)
+        step = 4096  # columns per chunk: no squared copy of the whole matrix
+        for c0 in range(0, prob.n, step):
+            c1 = min(prob.n, c0 + step)
+            a, b = int(L.ptr[c0]), int(L.ptr[c1])
+            if b == a:
+                continue
+            v = L.val[a:b]
+            starts = np.minimum(L.ptr[c0:c1] - a, b - a - 1)
+            out[c0:c1] += np.add.reduceat(v * v, starts) * (np.diff(L.ptr[c0:c1 + 1]) > 0)
     return out
 
 
@@ -114,20 +118,51 @@ def back_projection(ctx, b_k: np.ndarray, colnorm2: np.ndarray) -> np.ndarray:
     return np.where(colnorm2 > 0, v / np.maximum(colnorm2, 1e-300), 0.0)
 
 
-def model_instance(cfg, seed: int):
-    """x_true of the model class for one seed, and the synthetic parameters."""
-    rng = np.random.default_rng(10_000 + seed)
-    over = dict(seed=int(seed), n_blobs=int(rng.integers(16, 129)),
-                checker_amp=float(rng.uniform(0.0, 0.2)), checker_period=int(rng.integers(4, 17)))
-    p = params(cfg, **over)
-    x = np.empty(p.nx * p.ny * p.nz)
-    N.check(N.lib().plsqr_synth_xtrue(C.byref(p), N.ptr(x)), "plsqr_synth_xtrue")
-    return x, over
+def model_instance(grid, seed: int) -> np.ndarray:
+    """x_true of the model class for one seed (NumPy PCG64 stream of the
+    seed): 16-128 Gaussian blobs (sigma 3 cells, N(0,1) amplitudes, cut at 4
+    sigma) plus a +-a checkerboard, a in [0, 0.2], of period 4-16 cells."""
+    nx, ny, nz = grid
+    rng = np.random.default_rng(10_000 + int(seed))
+    nb = int(rng.integers(16, 129))
+    c = rng.uniform(0.0, 1.0, (nb, 3)) * np.array([nz, ny, nx])
+    amp = rng.standard_normal(nb)
+    period = int(rng.integers(4, 17))
+    a = float(rng.uniform(0.0, 0.2))
+    x = np.zeros((nz, ny, nx))
+    sig, r = 3.0, 12
+    for k in range(nb):
+        lo = np.maximum(c[k].astype(int) - r, 0)
+        hi = np.minimum(c[k].astype(int) + r + 1, [nz, ny, nx])
+        zz, yy, xx = np.ogrid[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]
+        d2 = (zz + 0.5 - c[k, 0]) ** 2 + (yy + 0.5 - c[k, 1]) ** 2 + (xx + 0.5 - c[k, 2]) ** 2
+        x[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]] += amp[k] * np.exp(-d2 / (2 * sig * sig))
+    half = max(period // 2, 1)
+    zz, yy, xx = np.ogrid[0:nz, 0:ny, 0:nx]
+    x += np.where((zz // half + yy // half + xx // half) % 2 == 0, a, -a)
+    return x.reshape(-1)
 
 
-def measurements(ctx, cfg, seed: int):
+def measurements(ctx, cfg, grid, seed: int):
     """(x_true, b_k) of one instance: the kernel product of x_true with 1%
-    noise drawn from the instance's seed."""
-    x, over = model_instance(cfg, seed)
-    kx = kernel_product(ctx, x)
-    return x, noisy(cfg, seed, kx)
+    noise drawn from the instance's seed (plsqr_synth_noisy)."""
+    x = model_instance(grid, seed)
+    return x, noisy(cfg, 50_000 + int(seed), kernel_product(ctx, x))
+
+
+def solve_batches(ctx, bs: list, inner: int, x0s=None, x_refs=None, k: int = 32):
+    """Batched mixed solves (one sweep of `inner` iterations) of the right-hand
+    sides bs, k at a time: (x list, history list, seconds per batch)."""
+    xs, hs, secs = [], [], []
+    for i in range(0, len(bs), k):
+        b = np.stack(bs[i:i + k])
+        kw = dict(sweeps=1, inner=inner)
+        if x0s is not None:
+            kw["x0"] = np.stack(x0s[i:i + k])
+        if x_refs is not None:
+            kw["x_ref"] = np.stack(x_refs[i:i + k])
+        out = ctx.batch_lsqr(b, **kw)
+        xs += list(out["x"])
+        hs += list(out["hist"])
+        secs.append(out["results"][0]["seconds"])
+    return xs, hs, secs
