@@ -175,6 +175,8 @@ def main() -> int:
     ap.add_argument("--train", type=int, default=2000, help="warm start: training pairs")
     ap.add_argument("--epochs", type=int, default=2, help="warm start: passes over the pairs")
     ap.add_argument("--heldout", type=int, default=200, help="warm start: held-out seeds")
+    ap.add_argument("--timed-single", type=int, default=4,
+                    help="warm start: held-out seeds also timed one at a time")
     ap.add_argument("--timed", type=int, default=16,
                     help="warm start: held-out seeds timed to 1e-6 against FP64 references")
     ap.add_argument("--extension", default=None, choices=["batched", "uneven", "warm"],
@@ -530,32 +532,46 @@ def bench_warm(pkg, args, device) -> dict:
             x_true, b = W.measurements(ctx, name, grid, s)
             bs.append(b)
             xt.append(x_true)
-            zs.append(W.back_projection(ctx, b, cn2))
+            zs.append(W.back_projection(ctx, b, cn2).astype(np.float32))
         return zs, bs, xt
 
     t0 = time.perf_counter()
     z_tr, b_tr, _ = inputs(seeds_train)
     x_tr, _, _ = W.solve_batches(ctx, b_tr, iters)
+    x_tr = [x.astype(np.float32) for x in x_tr]
+    del b_tr
     t_data = time.perf_counter() - t0
     log(f"training pairs: {len(x_tr)} in {t_data:.1f}s")
     # one global factor brings the solutions to the inputs' scale (the
     # network itself divides its input by, and multiplies its output with,
     # the input's root mean square)
     rms = lambda v: float(np.sqrt(np.mean(v * v)))
-    c = float(np.median([rms(x) / max(rms(z), 1e-300) for x, z in zip(x_tr, z_tr)]))
-    losses = []
+    c = float(np.median([rms(x.astype(np.float64)) / max(rms(z.astype(np.float64)), 1e-300)
+                         for x, z in zip(x_tr, z_tr)]))
+    z_te, b_te, _ = inputs(seeds_test)
+    x_te, _, _ = W.solve_batches(ctx, b_te, iters)
+
+    def rel_err(net, js):
+        return [float(np.linalg.norm(c * net.predict(z_te[j]) - x_te[j]) / np.linalg.norm(x_te[j]))
+                for j in js]
+
+    losses, curve = [], []
     t0 = time.perf_counter()
-    with W.UNet(grid, seed=1, device=device) as net:
-        for ep in range(args.epochs):
-            lr = 1e-3 if ep == 0 else 3e-4
-            order = np.random.default_rng(ep).permutation(len(z_tr))
-            for i in order:
-                losses.append(net.train_step(z_tr[i], x_tr[i] / c, lr))
-            log(f"epoch {ep}: mean loss {np.mean(losses[-len(order):]):.4f}")
-        t_train = time.perf_counter() - t0
-        z_te, b_te, _ = inputs(seeds_test)
-        x_te, _, _ = W.solve_batches(ctx, b_te, iters)
-        x0_te = [c * net.predict(z) for z in z_te]
+    net = W.UNet(grid, seed=1, device=device)
+    total, step = args.epochs * len(z_tr), 0
+    for ep in range(args.epochs):
+        order = np.random.default_rng(ep).permutation(len(z_tr))
+        for i in order:
+            # cosine decay of the step size from 1e-3 to 1e-5
+            lr = 1e-5 + 0.5 * (1e-3 - 1e-5) * (1.0 + np.cos(np.pi * step / total))
+            losses.append(net.train_step(z_tr[i], x_tr[i] / c, lr))
+            step += 1
+        e = float(np.median(rel_err(net, range(min(32, len(z_te))))))
+        curve.append({"epoch": ep, "loss": float(np.mean(losses[-len(order):])),
+                      "heldout_rel_err": e})
+        log(f"epoch {ep}: mean loss {curve[-1]['loss']:.4f}, held-out x0 error {e:.4f}")
+    t_train = time.perf_counter() - t0
+    x0_te = [c * net.predict(z) for z in z_te]
     pred_err = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(x0_te, x_te)]
     # timed subset: FP64 reference solutions (twice the iterations), then cold
     # and warm tracked runs
@@ -574,6 +590,48 @@ def bench_warm(pkg, args, device) -> dict:
     _, h_warm, s_warm = W.solve_batches(ctx, b_te[:nt], inner, x0s=x0_te[:nt], x_refs=xstar)
     k_cold = [first_below(h["err"], tol) for h in h_cold]
     k_warm = [first_below(h["err"], tol) for h in h_warm]
+    # how the savings grow with the accuracy of x0: the network's error
+    # scaled down by 10 and 100 (x0 = x* + t (x0_net - x*))
+    scaled = {}
+    if nt:
+        ts = (0.1, 0.01)
+        x0s = [xstar[j] + t * (x0_te[j] - xstar[j]) for t in ts for j in range(nt)]
+        _, h_sc, _ = W.solve_batches(ctx, b_te[:nt] * len(ts), inner, x0s=x0s,
+                                     x_refs=xstar * len(ts))
+        k_sc = [first_below(h["err"], tol) for h in h_sc]
+        for i, t in enumerate(ts):
+            ks = [k for k in k_sc[i * nt:(i + 1) * nt] if k is not None]
+            scaled[f"error_x{t:g}"] = float(np.mean(ks)) if ks else None
+    # one right-hand side at a time, as a user solves: device time to 1e-6
+    # of FP64 LSQR, of the mixed solve, and of back-projection + network +
+    # mixed solve from x0 (host wall time of the first two, with their copies)
+    single = []
+    with pkg.Context(prob, precision="mixed", device=device) as cm:
+        for j in range(min(args.timed_single, nt)):
+            if k64[j] is None:
+                continue
+            row = {"fp64": {"iterations": k64[j], "seconds": min(
+                ctx.lsqr(b_te[j], lsqr_iteration=k64[j])["result"]["seconds_total"]
+                for _ in range(2))}}
+            cm.set_reference_x(xstar[j])
+            kc = first_below(cm.lsqr(b_te[j], sweeps=1, inner=inner)["hist"]["err"], tol)
+            t0 = time.perf_counter()
+            x0 = c * net.predict(W.back_projection(ctx, b_te[j], cn2))
+            t_pre = time.perf_counter() - t0
+            hw = cm.lsqr(b_te[j], sweeps=1, inner=inner, x0=x0)
+            kw = first_below(hw["hist"]["err"], tol)
+            cm.set_reference_x(None)
+            if kc is None or kw is None:
+                continue
+            row["mixed"] = {"iterations": kc, "seconds": min(
+                cm.lsqr(b_te[j], sweeps=1, inner=kc)["result"]["seconds_total"]
+                for _ in range(2))}
+            row["mixed_warm"] = {"iterations": kw, "kept_x0": hw["result"]["warm"],
+                                 "x0_seconds": t_pre, "seconds": t_pre + min(
+                cm.lsqr(b_te[j], sweeps=1, inner=kw, x0=x0)["result"]["seconds_total"]
+                for _ in range(2))}
+            single.append(row)
+    net.close()
     ok = [a is not None and b is not None and c is not None for a, b, c in zip(k64, k_cold, k_warm)]
     sel = [j for j in range(nt) if ok[j]]
     out = {"metric": "iterations to 1e-6 rel. error (vs FP64 solution), held-out seeds: "
@@ -585,12 +643,14 @@ def bench_warm(pkg, args, device) -> dict:
                       "train_pairs": len(x_tr), "epochs": args.epochs,
                       "heldout": len(seeds_test), "timed": nt},
            "train_seconds": t_train, "data_seconds": t_data, "target_scale": c,
-           "loss_first_last": [float(np.mean(losses[:50])), float(np.mean(losses[-50:]))],
+           "training_curve": curve,
            "x0_rel_err_vs_x_lsqr": {"median": float(np.median(pred_err)),
                                     "p90": float(np.percentile(pred_err, 90))},
            "per_instance": [{"fp64": k64[j], "mixed_cold": k_cold[j], "mixed_warm": k_warm[j]}
                             for j in range(nt)],
            "fp64_iteration_ms": ms_fp64,
+           "iterations_with_x0_error_scaled": scaled,
+           "single_rhs": single,
            "seconds_total": time.perf_counter() - t_all}
     if sel:
         m64 = float(np.mean([k64[j] for j in sel]))
@@ -598,6 +658,14 @@ def bench_warm(pkg, args, device) -> dict:
         mw = float(np.mean([k_warm[j] for j in sel]))
         out.update(value=mw, mean_iterations={"fp64": m64, "mixed_cold": mc, "mixed_warm": mw},
                    warm_over_cold_iterations=mc / mw)
+    if single:
+        t64 = float(np.mean([r["fp64"]["seconds"] for r in single]))
+        out["time_to_1e-6_single_rhs"] = {
+            "instances": len(single), "fp64_s": t64,
+            "mixed_s": float(np.mean([r["mixed"]["seconds"] for r in single])),
+            "warm_mixed_s": float(np.mean([r["mixed_warm"]["seconds"] for r in single]))}
+        out["time_to_1e-6_single_rhs"]["speedup_warm_mixed_vs_fp64"] = \
+            t64 / out["time_to_1e-6_single_rhs"]["warm_mixed_s"]
     ctx.close()
     return out
 

@@ -113,6 +113,12 @@ typedef struct {
    * then holds sweeps * inner + 1 records and lsqr_iteration is unused.
    * damp > 0 requires sweeps = 1 (PLSQR_ERR_ARG otherwise).                 */
   int32_t sweeps, inner;
+  /* PLSQR_PREC_MIXED contexts only: starting solution x0 [n] (warm start) or
+   * NULL (x0 = 0, as in source/lsqr.c:311-312).  The first sweep corrects
+   * from r = b - A x0; where ||r|| is not below ||b|| the solve restarts
+   * from 0 (cold-start fallback) and plsqr_result.warm is 0.  Needs damp = 0
+   * (damping would regularise the correction, not the solution).           */
+  const double *x0;
 } plsqr_lsqr_args;
 
 /* Scalars of one iteration (index 0 = start-up, source/lsqr.c:343-445). */
@@ -127,7 +133,8 @@ typedef struct {
   int32_t istop, itn;
   double anorm, acond, rnorm, arnorm_out, xnorm;
   double arnorm, bnorm, dxmax;
-  int32_t maxdx, pad;
+  int32_t maxdx;
+  int32_t warm;         /* 1 when the solve started from the caller's x0     */
   double seconds;       /* device time of the iteration loop (CUDA events), the
                            region of the reference's "Parallel LSQR time"
                            (source/lsqr.c:476-842)                            */

@@ -53,13 +53,13 @@ class Info(C.Structure):
 class LsqrArgs(C.Structure):
     _fields_ = [("damp", f64), ("atol", f64), ("btol", f64), ("conlim", f64), ("itnlim", i32),
                 ("lsqr_iteration", i32), ("want_se", i32), ("stop_on_istop", i32),
-                ("result_txt", C.c_char_p), ("sweeps", i32), ("inner", i32)]
+                ("result_txt", C.c_char_p), ("sweeps", i32), ("inner", i32), ("x0", vp)]
 
 
 class Result(C.Structure):
     _fields_ = [("istop", i32), ("itn", i32), ("anorm", f64), ("acond", f64), ("rnorm", f64),
                 ("arnorm_out", f64), ("xnorm", f64), ("arnorm", f64), ("bnorm", f64),
-                ("dxmax", f64), ("maxdx", i32), ("pad", i32), ("seconds", f64),
+                ("dxmax", f64), ("maxdx", i32), ("warm", i32), ("seconds", f64),
                 ("seconds_total", f64)]
 
 

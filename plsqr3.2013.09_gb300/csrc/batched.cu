@@ -697,6 +697,7 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
       r.bnorm = c.bnorm;
       r.dxmax = c.dxmax;
       r.maxdx = c.maxdx;
+      r.warm = (int32_t)((warm >> j) & 1u);
       r.seconds = ms * 1e-3;
       r.seconds_total = r.seconds;
     }

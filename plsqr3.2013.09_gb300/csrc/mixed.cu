@@ -232,6 +232,11 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
                        "correction instead of the solution)");
     return PLSQR_ERR_ARG;
   }
+  const double *x0 = args->x0;
+  if (x0 && args->damp != 0.0) {
+    ctx_set_error(ctx, "x0 needs damp = 0 (damping would regularise the correction)");
+    return PLSQR_ERR_ARG;
+  }
   int rc;
   if ((rc = mixed_prepare(ctx))) return rc;
   MixedState *M = ctx->mixed;
@@ -251,7 +256,15 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   }
   if (ctx->m_k > 0)
     CK(cudaMemcpyAsync(M->b, b, sizeof(double) * ctx->m_k, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->n, ctx->stream));
+  // ||[b; 0]||, the residual norm of the cold start, for the warm-start test
+  double bnorm = 0.0;
+  if (x0) {
+    for (int32_t i = 0; i < ctx->m_k; ++i) bnorm += b[i] * b[i];
+    bnorm = sqrt(bnorm);
+    CK(cudaMemcpyAsync(ctx->x, x0, sizeof(double) * ctx->n, cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->n, ctx->stream));
+  }
   CK(cudaMemsetAsync(ctx->hist, 0, sizeof(plsqr_iter) * (total + 1), ctx->stream));
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   std::vector<plsqr_iter> hh((size_t)total + 1);
@@ -297,6 +310,13 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (s == 0 && x0 && !(cur.beta < bnorm)) {
+      // x0 does not lower the residual: start again from x = 0
+      x0 = nullptr;
+      CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->n, ctx->stream));
+      s = -1;
+      continue;
+    }
     if (s == 0) {
       plsqr_iter &h0 = hh[0];
       h0.alpha = cur.alpha;
@@ -306,6 +326,16 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
       h0.test1 = 1.0;
       h0.test2 = cur.beta > 0.0 ? cur.alpha / cur.beta : 0.0;
       h0.err = ctx->has_ref ? 1.0 : -1.0;
+      if (ctx->has_ref && x0) {  // the start is x0: its distance to the reference
+        std::vector<double> xr((size_t)ctx->n);
+        CK(cudaMemcpy(xr.data(), ctx->xref, sizeof(double) * ctx->n, cudaMemcpyDeviceToHost));
+        double d = 0.0, r2 = 0.0;
+        for (int32_t i = 0; i < ctx->n; ++i) {
+          d += (x0[i] - xr[(size_t)i]) * (x0[i] - xr[(size_t)i]);
+          r2 += xr[(size_t)i] * xr[(size_t)i];
+        }
+        h0.err = r2 > 0.0 ? sqrt(d / r2) : sqrt(d);
+      }
     }
     if (cur.done) break;  // A^T r = 0: x is a least-squares solution
     for (int i = 0; i < I; ++i) CK(cudaGraphLaunch(M->graph, ctx->stream));
@@ -341,6 +371,7 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   r.bnorm = cur.bnorm;
   r.dxmax = cur.dxmax;
   r.maxdx = cur.maxdx;
+  r.warm = x0 ? 1 : 0;
   r.seconds = ms * 1e-3;
   r.seconds_total = r.seconds;
   if (res) *res = r;

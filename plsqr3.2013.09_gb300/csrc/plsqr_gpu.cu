@@ -685,6 +685,11 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   if (!ctx || !args || args->lsqr_iteration < 0) return PLSQR_ERR_ARG;
   if (ctx->opts.precision == PLSQR_PREC_MIXED)
     return mixed_lsqr(ctx, args, b_k, x, w, se, hist, res);
+  if (args->x0) {
+    ctx_set_error(ctx, "x0 needs a mixed-precision context (the FP64 path starts from 0, as "
+                       "source/lsqr.c:311-312 does)");
+    return PLSQR_ERR_ARG;
+  }
   const double *b = b_k;
   if (!b) {
     if ((int32_t)ctx->b_k.size() != ctx->m_k) return PLSQR_ERR_STATE;

@@ -140,7 +140,11 @@ class Context:
              atol: float = 1e-10, btol: float = 1e-10, conlim: float = 100.0,
              itnlim: int = 1000, want_se: bool = False, stop_on_istop: bool = False,
              result_txt: str | None = None, sweeps: int = 4, inner: int = 50,
-             want_w: bool = False) -> dict:
+             want_w: bool = False, x0=None) -> dict:
+        """One solve (source/lsqr.c:195-917).  Mixed-precision contexts take
+        `sweeps` x `inner` iterations instead of lsqr_iteration, and x0 (n,):
+        a starting solution, kept when it lowers the residual
+        (result["warm"] == 1), else the solve starts from 0."""
         a = N.LsqrArgs()
         N.lib().plsqr_default_lsqr_args(C.byref(a))
         a.damp, a.atol, a.btol, a.conlim = damp, atol, btol, conlim
@@ -148,6 +152,8 @@ class Context:
         a.want_se, a.stop_on_istop = int(want_se), int(stop_on_istop)
         a.result_txt = result_txt.encode() if result_txt else None
         a.sweeps, a.inner = sweeps, inner
+        xs = None if x0 is None else _f64(x0, self.n, "x0")
+        a.x0 = N.ptr(xs)
         b = self._b if b_k is None else _f64(b_k, self.m_k, "b_k")
         n_hist = (sweeps * inner if self.precision == "mixed" else lsqr_iteration) + 1
         x = np.empty(self.n)

@@ -238,3 +238,33 @@ def test_mixed_precision_refuses_damped_refinement(pkg, problems):
         assert e.value.code == -1
         out = cm.lsqr(damp=0.1, sweeps=1, inner=10)
         assert np.all(np.isfinite(out["x"]))
+
+
+def test_mixed_precision_warm_start(pkg, problems):
+    """x0 near the solution is kept and saves iterations; an x0 that raises
+    the residual falls back to the cold start, bit for bit; the FP64 path and
+    damped solves refuse x0."""
+    prob = problems("grid32")
+    with pkg.Context(prob) as c64:
+        xstar = c64.lsqr(lsqr_iteration=400)["x"]
+        with pytest.raises(pkg._native.PlsqrError) as e:
+            c64.lsqr(lsqr_iteration=5, x0=xstar)
+        assert e.value.code == -1
+    rng = np.random.default_rng(3)
+    with pkg.Context(prob, precision="mixed") as cm:
+        cm.set_reference_x(xstar)
+        cold = cm.lsqr(sweeps=2, inner=200)
+        x0 = xstar + 1e-3 * np.linalg.norm(xstar) / np.sqrt(prob.n) * rng.standard_normal(prob.n)
+        warm = cm.lsqr(sweeps=2, inner=200, x0=x0)
+        assert cold["result"]["warm"] == 0 and warm["result"]["warm"] == 1
+        assert abs(warm["hist"]["err"][0] - rel(x0, xstar)) <= 1e-12
+        k_cold = int(np.argmax(cold["hist"]["err"] <= 1e-6))
+        k_warm = int(np.argmax(warm["hist"]["err"] <= 1e-6))
+        assert 0 < k_warm < k_cold
+        bad = cm.lsqr(sweeps=2, inner=200, x0=1e6 * rng.standard_normal(prob.n))
+        assert bad["result"]["warm"] == 0
+        assert np.array_equal(bad["x"], cold["x"])
+        assert np.array_equal(bad["hist"]["err"], cold["hist"]["err"])
+        with pytest.raises(pkg._native.PlsqrError) as e:
+            cm.lsqr(damp=0.1, sweeps=1, inner=10, x0=x0)
+        assert e.value.code == -1
