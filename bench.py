@@ -173,7 +173,7 @@ def main() -> int:
                     help="profiling run: build the context, run one short solve, exit")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--train", type=int, default=2000, help="warm start: training pairs")
-    ap.add_argument("--epochs", type=int, default=2, help="warm start: passes over the pairs")
+    ap.add_argument("--epochs", type=int, default=6, help="warm start: passes over the pairs")
     ap.add_argument("--heldout", type=int, default=200, help="warm start: held-out seeds")
     ap.add_argument("--timed-single", type=int, default=4,
                     help="warm start: held-out seeds also timed one at a time")
@@ -244,6 +244,18 @@ def main() -> int:
         with pkg.multi.Multi(probs, device=local) as mp:
             out = mp.solve()
         log(f"profile run: 24 uneven problems, {out['seconds'] * 1e3:.2f} ms")
+        return 0
+    if args.profile and args.extension == "warm":
+        # the network alone on the 96x96x32 grid: three training steps and a
+        # prediction on seeded volumes (no operator needed)
+        grid = (96, 96, 32)
+        rng = np.random.default_rng(5)
+        z = rng.standard_normal(96 * 96 * 32).astype(np.float32)
+        with pkg.warm.UNet(grid, seed=1, device=local) as net:
+            for _ in range(3):
+                net.train_step(z, np.roll(z, 1), 1e-3)
+            net.predict(z)
+        log("profile run: U-Net 96x96x32, 3 training steps + 1 prediction")
         return 0
     if args.profile:
         prob = pkg.generate(args.config)

@@ -2,12 +2,12 @@
 //
 // Activations are channels-last BF16 blocks X[voxel][C] (voxel = (z*ny +
 // y)*nx + x, the column order of the model), C a multiple of 16.  A 3x3x3
-// convolution is im2col (Col[voxel][tap*C + c], zero outside the grid) and a
-// tensor-core GEMM; its backward passes are GEMMs on transposed blocks plus a
-// gathering col2im.  The GEMM is C[M][N] = sum_k A[m][k] B[n][k] with BF16
-// operands (k contiguous in both) and FP32 accumulation, on mma.sync
-// m16n8k16: these contractions are a few GFLOP per volume, far from the hot
-// path of the solver.
+// convolution and its input gradient are implicit GEMMs on the tcgen05
+// tensor cores (conv_tc.cuh).  The weight gradient dW[co][tap*C + c] =
+// sum_p dz[p][co] X[p + offset(tap)][c] goes through im2col (Col[voxel][tap*C
+// + c], zero outside the grid), transposes and the GEMM here: C[M][N] =
+// sum_k A[m][k] B[n][k] with BF16 operands (k contiguous in both) and FP32
+// accumulation on mma.sync m16n8k16, split over the voxel range.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -148,24 +148,6 @@ __global__ void k_im2col(const __nv_bfloat16 *__restrict__ X, Grid3 g, int C,
   }
 }
 
-// dX[p][c] = sum over taps t of dCol[p - offset(t)][t*C + c] (neighbours inside).
-__global__ void k_col2im(const float *__restrict__ dcol, Grid3 g, int C, float *__restrict__ dX) {
-  const int64_t K = 27LL * C, total = g.n() * C;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    const int64_t p = i / C;
-    const int x = (int)(p % g.nx), y = (int)((p / g.nx) % g.ny), z = (int)(p / ((int64_t)g.nx * g.ny));
-    float s = 0.f;
-    for (int t = 0; t < 27; ++t) {
-      const int xx = x - (t % 3 - 1), yy = y - ((t / 3) % 3 - 1), zz = z - (t / 9 - 1);
-      if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz)
-        s += dcol[(((int64_t)zz * g.ny + yy) * g.nx + xx) * K + (int64_t)t * C + c];
-    }
-    dX[i] = s;
-  }
-}
-
 // out[c][r] = in[r][c] for a rows x cols BF16 block (32 x 32 tiles).
 __global__ void k_transpose_bf16(const __nv_bfloat16 *__restrict__ in, int64_t rows, int64_t cols,
                                  __nv_bfloat16 *__restrict__ out) {
@@ -186,19 +168,6 @@ __global__ void k_f32_to_bf16(const float *__restrict__ in, int64_t n, __nv_bflo
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     out[i] = __float2bfloat16(in[i]);
-}
-
-// act[p][c] = bf16(max(0, y[p][c] + bias[c])) (relu = 0: no clamp); also
-// the FP32 value when keep is given.
-__global__ void k_bias_act(const float *__restrict__ y, const float *__restrict__ bias, int64_t n,
-                           int C, int relu, __nv_bfloat16 *__restrict__ act) {
-  const int64_t total = n * C;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float v = y[i] + bias[i % C];
-    if (relu) v = fmaxf(v, 0.f);
-    act[i] = __float2bfloat16(v);
-  }
 }
 
 // dz[p][c] = bf16(d[p][c] * (act[p][c] > 0)), the gradient through the ReLU.

@@ -1,9 +1,11 @@
 // The warm-start network: a 3-D U-Net (3 levels, 16/32/64 channels) from the
 // column-norm-scaled back-projection A^T b to a starting solution x0 on the
 // model grid, trained on (A^T b, x_LSQR) pairs that this library's solvers
-// produce.  Weights are FP32 masters with BF16 copies; convolutions are
-// im2col + BF16 tensor-core GEMMs with FP32 accumulation (nn_kernels.cuh);
-// one volume per step, Adam.
+// produce.  Weights are FP32 masters with BF16 copies.  The forward
+// convolutions and their input gradients are implicit GEMMs on the tcgen05
+// tensor cores (BF16 operands, FP32 accumulation in tensor memory,
+// conv_tc.cuh); the weight gradients are im2col + BF16 mma.sync GEMMs
+// (nn_kernels.cuh).  One volume per step, Adam.
 //
 //   x16 = input / s (channel 0 of 16)                          level 0
 //   e1 = relu(conv(relu(conv(x16, 16)), 16))                   level 0
@@ -22,6 +24,7 @@
 #include <memory>
 #include <vector>
 
+#include "conv_tc.cuh"
 #include "nn_kernels.cuh"
 #include "plsqr_gpu.h"
 
@@ -70,8 +73,8 @@ struct plsqr_unet {
       *g_d1a, *g_d1b;
   // scratch
   bf16 *col = nullptr, *colt = nullptr, *dz = nullptr, *dzt = nullptr;
-  float *y = nullptr, *dcol = nullptr, *part = nullptr, *in = nullptr, *out = nullptr,
-        *target = nullptr, *hparts = nullptr;
+  float *part = nullptr, *in = nullptr, *out = nullptr, *target = nullptr, *hparts = nullptr;
+  unsigned int *dflag = nullptr;  // set by a tensor-core convolution whose wait ran out
   int64_t step = 0;
   char err[256] = {0};
 };
@@ -156,16 +159,78 @@ int gemm(plsqr_unet *net, const bf16 *A, int64_t lda, const bf16 *B, int64_t ldb
   return PLSQR_OK;
 }
 
-// act = relu(conv(x) + b) (relu = 0: no clamp).
-int conv_fwd(plsqr_unet *net, Conv &L, const bf16 *x, bf16 *act) {
-  cudaStream_t s = net->stream;
-  const int64_t n = L.g.n(), K = L.K();
-  k_im2col<<<grid_for(n * 27 * (L.cin / 8)), kT, 0, s>>>(x, L.g, L.cin, net->col);
-  int rc;
-  if ((rc = gemm(net, net->col, K, L.wb, K, net->y, n, L.cout, K, 1))) return rc;
-  k_bias_act<<<grid_for(n * L.cout), kT, 0, s>>>(net->y, L.b, n, L.cout, 1, act);
+template <int CI, int CO>
+int conv_tc_run(plsqr_unet *net, const ConvTcArgs &a) {
+  using S = ConvTcShape<CI, CO>;
+  // at most 512 / cols CTAs per SM (of 228 KB of shared memory), so that
+  // every resident CTA's tensor-memory allocation succeeds at once
+  constexpr uint32_t cols = tc_cols(CO);
+  constexpr int floor_bytes = cols >= 128 ? 58 * 1024 : cols >= 64 ? 30 * 1024 : 0;
+  constexpr int bytes = S::kSmemBytes > floor_bytes ? S::kSmemBytes : floor_bytes;
+  static_assert(bytes <= 227 * 1024, "shared memory of one CTA");
+  UK(cudaFuncSetAttribute(k_conv_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  const int64_t blocks = (a.g.n() + kTcRows - 1) / kTcRows;
+  k_conv_tc<CI, CO><<<(unsigned)blocks, kTcThreads, bytes, net->stream>>>(a);
   UK(cudaGetLastError());
   return PLSQR_OK;
+}
+
+// The channel pairs of the network's layers (forward: cin -> cout; input
+// gradient: cout -> cin).
+int conv_tc(plsqr_unet *net, int ci, int co, const ConvTcArgs &a) {
+#define PLSQR_TC_PAIR(I, O) \
+  if (ci == I && co == O) return conv_tc_run<I, O>(net, a);
+  PLSQR_TC_PAIR(16, 16)
+  PLSQR_TC_PAIR(16, 32)
+  PLSQR_TC_PAIR(32, 32)
+  PLSQR_TC_PAIR(32, 64)
+  PLSQR_TC_PAIR(64, 64)
+  PLSQR_TC_PAIR(96, 32)
+  PLSQR_TC_PAIR(48, 16)
+  PLSQR_TC_PAIR(32, 16)
+  PLSQR_TC_PAIR(64, 32)
+  PLSQR_TC_PAIR(32, 96)
+  PLSQR_TC_PAIR(16, 48)
+#undef PLSQR_TC_PAIR
+  snprintf(net->err, sizeof net->err, "no tensor-core convolution for %d -> %d channels", ci, co);
+  return PLSQR_ERR_ARG;
+}
+
+bool conv_tc_supported(int cin, int cout) {
+  const int pairs[][2] = {{16, 16}, {16, 32}, {32, 32}, {32, 64}, {64, 64}, {96, 32}, {48, 16}};
+  for (auto &p : pairs)
+    if (p[0] == cin && p[1] == cout) return true;
+  return false;
+}
+
+// The device flag of the tensor-core convolutions, after the stream has
+// drained: PLSQR_ERR_TIMEOUT (and the flag cleared) when a wait ran out.
+int check_flag(plsqr_unet *net) {
+  unsigned int f = 0;
+  UK(cudaMemcpy(&f, net->dflag, sizeof f, cudaMemcpyDeviceToHost));
+  if (f) {
+    UK(cudaMemset(net->dflag, 0, sizeof f));
+    snprintf(net->err, sizeof net->err,
+             "a tensor-core convolution's wait on its MMAs ran out (one second)");
+    return PLSQR_ERR_TIMEOUT;
+  }
+  return PLSQR_OK;
+}
+
+// act = relu(conv(x) + b): one implicit-GEMM launch.
+int conv_fwd(plsqr_unet *net, Conv &L, const bf16 *x, bf16 *act) {
+  ConvTcArgs a{};
+  a.x = x;
+  a.w = L.wb;  // B_t[co][ci] = wb[co][t*cin + ci]
+  a.ldw = L.K();
+  a.tap_stride = L.cin;
+  a.flip = 0;
+  a.bias = L.b;
+  a.relu = 1;
+  a.out_bf16 = act;
+  a.g = L.g;
+  a.err = net->dflag;
+  return conv_tc(net, L.cin, L.cout, a);
 }
 
 // The gradients of one layer from d(act) (FP32 [n][cout]): gw, gb, and dx
@@ -188,12 +253,21 @@ int conv_bwd(plsqr_unet *net, Conv &L, const bf16 *x, const bf16 *act, const flo
   const int splits = (int)std::min<int64_t>(64, std::max<int64_t>(1, n / 4096));
   if ((rc = gemm(net, net->dzt, n, net->colt, n, L.gw, L.cout, K, n, splits))) return rc;
   if (dx) {
-    // dCol[p][k] = sum_co dz[p][co] W[co][k]; dx = col2im(dCol)
+    // dx[p][ci] = sum_t sum_co dz[p - offset(t)][co] W[co][t*cin + ci]: the
+    // implicit GEMM on dz with mirrored taps and B_t[ci][co] = wbt[t*cin + ci][co]
     k_transpose_bf16<<<dim3((unsigned)((K + 31) / 32), (unsigned)((L.cout + 31) / 32)), tb, 0, s>>>(
         L.wb, L.cout, K, L.wbt);
-    if ((rc = gemm(net, net->dz, L.cout, L.wbt, L.cout, net->dcol, n, K, L.cout, 1))) return rc;
-    k_col2im<<<grid_for(n * L.cin), kT, 0, s>>>(net->dcol, L.g, L.cin, dx);
     UK(cudaGetLastError());
+    ConvTcArgs a{};
+    a.x = net->dz;
+    a.w = L.wbt;
+    a.ldw = L.cout;
+    a.tap_stride = (int64_t)L.cin * L.cout;
+    a.flip = 1;
+    a.out_f32 = dx;
+    a.g = L.g;
+    a.err = net->dflag;
+    if ((rc = conv_tc(net, L.cout, L.cin, a))) return rc;
   }
   return PLSQR_OK;
 }
@@ -240,6 +314,7 @@ int forward(plsqr_unet *net, float s) {
   float hb = 0.f;
   UK(cudaMemcpyAsync(&hb, net->hw + 16, sizeof(float), cudaMemcpyDeviceToHost, st));
   UK(cudaStreamSynchronize(st));
+  if ((rc = check_flag(net))) return rc;
   k_head<<<grid_for(n0), kT, 0, st>>>(net->a_d1b, n0, 16, net->hw, hb, s, net->out);
   UK(cudaGetLastError());
   return PLSQR_OK;
@@ -282,6 +357,7 @@ int backward(plsqr_unet *net, float s, float lr, float *loss) {
     return rc;
   UK(cudaGetLastError());
   UK(cudaStreamSynchronize(st));
+  if ((rc = check_flag(net))) return rc;
   // head gradient (fixed order over the partials) and the loss
   float hg[17] = {0.f}, se = 0.f;
   for (int b = 0; b < hgrid; ++b) {
@@ -319,9 +395,8 @@ namespace {
 int alloc_scratch(plsqr_unet *net, int64_t max_nk, int64_t max_ncout, int64_t max_wk) {
   int rc;
   if ((rc = nalloc(net, &net->col, max_nk)) || (rc = nalloc(net, &net->colt, max_nk)) ||
-      (rc = nalloc(net, &net->dcol, max_nk)) || (rc = nalloc(net, &net->dz, max_ncout)) ||
-      (rc = nalloc(net, &net->dzt, max_ncout)) || (rc = nalloc(net, &net->y, max_ncout)) ||
-      (rc = nalloc(net, &net->part, 64 * max_wk)))
+      (rc = nalloc(net, &net->dz, max_ncout)) || (rc = nalloc(net, &net->dzt, max_ncout)) ||
+      (rc = nalloc(net, &net->part, 64 * max_wk)) || (rc = nalloc(net, &net->dflag, 1)))
     return rc;
   return PLSQR_OK;
 }
@@ -487,8 +562,8 @@ extern "C" int plsqr_nn_conv3d_check(int32_t nx, int32_t ny, int32_t nz, int32_t
                                      int32_t cout, const float *x, const float *w,
                                      const float *b, const float *dy, float *y, float *dx,
                                      float *dw, float *db) {
-  if (nx < 1 || ny < 1 || nz < 1 || cin < 16 || cin % 16 || cout < 16 || cout % 16 ||
-      cout > 64 || ((int64_t)nx * ny * nz) % 8 || !x || !w || !b || !dy || !y || !dx || !dw || !db)
+  if (nx < 1 || ny < 1 || nz < 1 || !conv_tc_supported(cin, cout) ||
+      ((int64_t)nx * ny * nz) % 8 || !x || !w || !b || !dy || !y || !dx || !dw || !db)
     return PLSQR_ERR_ARG;
   int32_t ndev = 0;
   plsqr_device_count(&ndev);
@@ -535,6 +610,7 @@ extern "C" int plsqr_nn_conv3d_check(int32_t nx, int32_t ny, int32_t nz, int32_t
       rc = PLSQR_ERR_CUDA;
       break;
     }
+    if ((rc = check_flag(net))) break;
     for (int64_t i = 0; i < n * cout; ++i) y[i] = __bfloat162float(hb[(size_t)i]);
   } while (0);
   free_net(net);
