@@ -4,10 +4,8 @@
 // y)*nx + x, the column order of the model), C a multiple of 16.  A 3x3x3
 // convolution and its input gradient are implicit GEMMs on the tcgen05
 // tensor cores (conv_tc.cuh).  The weight gradient dW[co][tap*C + c] =
-// sum_p dz[p][co] X[p + offset(tap)][c] goes through im2col (Col[voxel][tap*C
-// + c], zero outside the grid), transposes and the GEMM here: C[M][N] =
-// sum_k A[m][k] B[n][k] with BF16 operands (k contiguous in both) and FP32
-// accumulation on mma.sync m16n8k16, split over the voxel range.
+// sum_p dz[p][co] X[p + offset(tap)][c] is a tcgen05 GEMM (conv_tc.cuh) on
+// the transposed im2col block written here (k_im2col_t) and dz transposed.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -16,135 +14,48 @@
 namespace plsqr {
 namespace nn {
 
-constexpr int kGemmThreads = 128;  // four warps, 2 x 2 over a 64 x 64 tile
-constexpr int kBM = 64, kBN = 64, kBK = 32, kPad = 8;
-
-__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint32_t *b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-// A tile of kBM (or kBN) rows by kBK k's into shared memory, zeros outside
-// [0, rows) x [k0, k1).  Each thread moves 16 bf16 (two 16-byte loads); the
-// callers keep lda a multiple of 8 and k0, k1 multiples of 8.
-__device__ __forceinline__ void load_tile(const __nv_bfloat16 *__restrict__ g, int64_t ld,
-                                          int64_t row0, int64_t rows, int64_t k0, int64_t k1,
-                                          __nv_bfloat16 (*s)[kBK + kPad]) {
-  const int r = threadIdx.x >> 1, half = threadIdx.x & 1;
-  const int64_t row = row0 + r;
-  uint4 v[2];
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const int64_t k = k0 + half * 16 + q * 8;
-    if (row < rows && k < k1)
-      v[q] = *reinterpret_cast<const uint4 *>(g + row * ld + k);
-    else
-      v[q] = make_uint4(0, 0, 0, 0);
-  }
-  uint4 *d = reinterpret_cast<uint4 *>(&s[r][half * 16]);
-  d[0] = v[0];
-  d[1] = v[1];
-}
-
-// C[z][M][N] = sum over k in [z*kchunk, min(K, (z+1)*kchunk)) of A[m][k] B[n][k].
-// Grid (ceil(M/64), ceil(N/64), splits).  kchunk a multiple of kBK.
-__global__ void __launch_bounds__(kGemmThreads)
-    k_gemm_nt(const __nv_bfloat16 *__restrict__ A, int64_t lda, const __nv_bfloat16 *__restrict__ B,
-              int64_t ldb, float *__restrict__ C, int64_t M, int64_t N, int64_t K,
-              int64_t kchunk) {
-  __shared__ __align__(16) __nv_bfloat16 As[kBM][kBK + kPad];
-  __shared__ __align__(16) __nv_bfloat16 Bs[kBN][kBK + kPad];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int wm = warp >> 1, wn = warp & 1;
-  const int gid = lane >> 2, tig = lane & 3;
-  const int64_t m0 = (int64_t)blockIdx.x * kBM, n0 = (int64_t)blockIdx.y * kBN;
-  const int64_t kb = (int64_t)blockIdx.z * kchunk;
-  const int64_t ke = kb + kchunk < K ? kb + kchunk : K;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-  for (int64_t k0 = kb; k0 < ke; k0 += kBK) {
-    load_tile(A, lda, m0, M, k0, ke, As);
-    load_tile(B, ldb, n0, N, k0, ke, Bs);
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < kBK; kk += 16) {
-      uint32_t a[2][4], b[4][2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r = wm * 32 + i * 16 + gid;
-        a[i][0] = *reinterpret_cast<const uint32_t *>(&As[r][kk + tig * 2]);
-        a[i][1] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + tig * 2]);
-        a[i][2] = *reinterpret_cast<const uint32_t *>(&As[r][kk + tig * 2 + 8]);
-        a[i][3] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + tig * 2 + 8]);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int c = wn * 32 + j * 8 + gid;
-        b[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + tig * 2]);
-        b[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + tig * 2 + 8]);
-      }
-#pragma unroll
-      for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], a[i], b[j]);
-    }
-    __syncthreads();
-  }
-  float *Cz = C + (int64_t)blockIdx.z * M * N;
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int64_t r = m0 + wm * 32 + i * 16 + gid;
-      const int64_t c = n0 + wn * 32 + j * 8 + tig * 2;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int64_t rr = r + (q >= 2 ? 8 : 0), cc = c + (q & 1);
-        if (rr < M && cc < N) Cz[rr * N + cc] = acc[i][j][q];
-      }
-    }
-}
-
-// out[i] = sum over z of part[z][i] (fixed order).
-__global__ void k_sum_splits(const float *__restrict__ part, int64_t count, int splits,
-                             float *__restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (int z = 0; z < splits; ++z) s += part[(int64_t)z * count + i];
-    out[i] = s;
-  }
-}
-
 struct Grid3 {
   int nx, ny, nz;
   __host__ __device__ int64_t n() const { return (int64_t)nx * ny * nz; }
 };
 
-// Col[p][t*C + c] = X[p + offset(t)][c] (zero outside), t = (dz+1)*9 + (dy+1)*3 + dx+1.
-__global__ void k_im2col(const __nv_bfloat16 *__restrict__ X, Grid3 g, int C,
-                         __nv_bfloat16 *__restrict__ col) {
-  const int64_t K = 27LL * C, total = g.n() * 27 * (C / 8);
+// Colt[t*C + c][p] = X[p + offset(t)][c] (zero outside the grid): the
+// transposed im2col block of the weight gradient, written directly.  A
+// thread takes two neighbouring voxels and one tap, reads their channel rows
+// in 16-byte pieces and writes bf16 pairs down the C rows, so that a warp
+// writes 128 contiguous bytes of each row.  n must be even.
+__global__ void k_im2col_t(const __nv_bfloat16 *__restrict__ X, Grid3 g, int C,
+                           __nv_bfloat16 *__restrict__ colt) {
+  const int64_t n = g.n(), half = n / 2, total = 27 * half;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int c8 = (int)(i % (C / 8));
-    const int64_t pt = i / (C / 8);
-    const int t = (int)(pt % 27);
-    const int64_t p = pt / 27;
-    const int x = (int)(p % g.nx), y = (int)((p / g.nx) % g.ny), z = (int)(p / ((int64_t)g.nx * g.ny));
-    const int xx = x + t % 3 - 1, yy = y + (t / 3) % 3 - 1, zz = z + t / 9 - 1;
-    uint4 v = make_uint4(0, 0, 0, 0);
-    if (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz)
-      v = *reinterpret_cast<const uint4 *>(X + (((int64_t)zz * g.ny + yy) * g.nx + xx) * C + c8 * 8);
-    *reinterpret_cast<uint4 *>(col + p * K + (int64_t)t * C + c8 * 8) = v;
+    const int t = (int)(i / half);
+    const int64_t p = 2 * (i % half);
+    const int ox = t % 3 - 1, oy = (t / 3) % 3 - 1, oz = t / 9 - 1;
+    const __nv_bfloat16 *src[2];
+    for (int v = 0; v < 2; ++v) {
+      const int64_t q = p + v;
+      const int x = (int)(q % g.nx), y = (int)((q / g.nx) % g.ny), z = (int)(q / ((int64_t)g.nx * g.ny));
+      const int xx = x + ox, yy = y + oy, zz = z + oz;
+      src[v] = (xx >= 0 && xx < g.nx && yy >= 0 && yy < g.ny && zz >= 0 && zz < g.nz)
+                   ? X + (((int64_t)zz * g.ny + yy) * g.nx + xx) * C
+                   : nullptr;
+    }
+    __nv_bfloat16 *dst = colt + (int64_t)t * C * n + p;
+    for (int c8 = 0; c8 < C; c8 += 8) {
+      uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
+      if (src[0]) a = *reinterpret_cast<const uint4 *>(src[0] + c8);
+      if (src[1]) b = *reinterpret_cast<const uint4 *>(src[1] + c8);
+      const __nv_bfloat16 *ea = reinterpret_cast<const __nv_bfloat16 *>(&a);
+      const __nv_bfloat16 *eb = reinterpret_cast<const __nv_bfloat16 *>(&b);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        __nv_bfloat162 pr;
+        pr.x = ea[c];
+        pr.y = eb[c];
+        *reinterpret_cast<__nv_bfloat162 *>(dst + (int64_t)(c8 + c) * n) = pr;
+      }
+    }
   }
 }
 
@@ -178,20 +89,37 @@ __global__ void k_relu_back(const float *__restrict__ d, const __nv_bfloat16 *__
     dz[i] = __float2bfloat16(__bfloat162float(act[i]) > 0.f ? d[i] : 0.f);
 }
 
-// db[c] = sum over voxels of dz[p][c] (one block per channel, fixed order).
-__global__ void k_bias_grad(const __nv_bfloat16 *__restrict__ dz, int64_t n, int C,
-                            float *__restrict__ db) {
-  __shared__ float red[256];
-  const int c = blockIdx.x;
+// db[c] = sum over voxels of dz[p][c], in two fixed-order steps: each block
+// of kBiasThreads threads reads a grid-strided share of dz in storage order
+// (a thread keeps one channel, as kBiasThreads * gridDim is a multiple of
+// C) and writes its per-channel sums to parts[block][C]; k_bias_grad_final
+// adds the blocks' sums in block order.
+constexpr int kBiasThreads = 192;  // a multiple of 16, 32, 48, 64 and 96
+
+__global__ void __launch_bounds__(kBiasThreads)
+    k_bias_grad(const __nv_bfloat16 *__restrict__ dz, int64_t n, int C, float *__restrict__ parts) {
+  __shared__ float red[kBiasThreads];
+  const int64_t total = n * C, stride = (int64_t)gridDim.x * kBiasThreads;
   float s = 0.f;
-  for (int64_t p = threadIdx.x; p < n; p += blockDim.x) s += __bfloat162float(dz[p * C + c]);
+  for (int64_t i = blockIdx.x * (int64_t)kBiasThreads + threadIdx.x; i < total; i += stride)
+    s += __bfloat162float(dz[i]);
   red[threadIdx.x] = s;
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
+  // thread c < C sums the threads of channel c (c, c + C, ...) in order
+  if ((int)threadIdx.x < C) {
+    float t = 0.f;
+    for (int k = threadIdx.x; k < kBiasThreads; k += C) t += red[k];
+    parts[(int64_t)blockIdx.x * C + threadIdx.x] = t;
   }
-  if (threadIdx.x == 0) db[c] = red[0];
+}
+
+__global__ void k_bias_grad_final(const float *__restrict__ parts, int blocks, int C,
+                                  float *__restrict__ db) {
+  const int c = threadIdx.x;
+  if (c >= C) return;
+  float t = 0.f;
+  for (int b = 0; b < blocks; ++b) t += parts[(int64_t)b * C + c];
+  db[c] = t;
 }
 
 // 2x2x2 average pooling of a channels-last block (fine grid g).

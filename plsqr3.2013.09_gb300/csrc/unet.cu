@@ -34,6 +34,7 @@ typedef __nv_bfloat16 bf16;
 namespace {
 
 constexpr int kT = 256;  // threads of the elementwise kernels
+constexpr int kBiasBlocks = 304;  // blocks of the bias-gradient reduction
 
 int grid_for(int64_t work) {
   int64_t g = (work + kT - 1) / kT;
@@ -72,9 +73,11 @@ struct plsqr_unet {
   float *g_e1a, *g_e1b, *g_p1, *g_e2a, *g_e2b, *g_p2, *g_ba, *g_bb, *g_c2, *g_d2a, *g_d2b, *g_c1,
       *g_d1a, *g_d1b;
   // scratch
-  bf16 *col = nullptr, *colt = nullptr, *dz = nullptr, *dzt = nullptr;
-  float *part = nullptr, *in = nullptr, *out = nullptr, *target = nullptr, *hparts = nullptr;
-  unsigned int *dflag = nullptr;  // set by a tensor-core convolution whose wait ran out
+  bf16 *colt = nullptr, *dz = nullptr, *dzt = nullptr;
+  float *part = nullptr, *in = nullptr, *out = nullptr, *target = nullptr, *hparts = nullptr,
+        *bparts = nullptr;
+  unsigned int *dflag = nullptr;  // set by a tensor-core kernel whose wait ran out
+  int64_t part_cap = 0;           // floats of part
   int64_t step = 0;
   char err[256] = {0};
 };
@@ -136,41 +139,29 @@ int init_conv(plsqr_unet *net, Conv &L, int cin, int cout, Grid3 g, int fan_c, u
   return PLSQR_OK;
 }
 
-}  // namespace
-
-namespace {
-
-// C[M][N] = A[M][K] . B[N][K]^T with `splits` chunks of the K range summed
-// in order into C (part holds splits * M * N floats when splits > 1).
-int gemm(plsqr_unet *net, const bf16 *A, int64_t lda, const bf16 *B, int64_t ldb, float *C,
-         int64_t M, int64_t N, int64_t K, int splits) {
-  cudaStream_t s = net->stream;
-  int64_t kc = (K + splits - 1) / splits;
-  kc = (kc + kBK - 1) / kBK * kBK;
-  const int z = (int)((K + kc - 1) / kc);
-  dim3 grid((unsigned)((M + kBM - 1) / kBM), (unsigned)((N + kBN - 1) / kBN), (unsigned)z);
-  if (z == 1) {
-    k_gemm_nt<<<grid, kGemmThreads, 0, s>>>(A, lda, B, ldb, C, M, N, K, kc);
-  } else {
-    k_gemm_nt<<<grid, kGemmThreads, 0, s>>>(A, lda, B, ldb, net->part, M, N, K, kc);
-    k_sum_splits<<<grid_for(M * N), kT, 0, s>>>(net->part, M * N, z, C);
-  }
-  UK(cudaGetLastError());
-  return PLSQR_OK;
-}
-
+// The halo-staged kernel where its halo and all 27 weight taps fit in one
+// CTA's shared memory, else the kernel that gathers tap by tap.
 template <int CI, int CO>
 int conv_tc_run(plsqr_unet *net, const ConvTcArgs &a) {
-  using S = ConvTcShape<CI, CO>;
   // at most 512 / cols CTAs per SM (of 228 KB of shared memory), so that
   // every resident CTA's tensor-memory allocation succeeds at once
   constexpr uint32_t cols = tc_cols(CO);
   constexpr int floor_bytes = cols >= 128 ? 58 * 1024 : cols >= 64 ? 30 * 1024 : 0;
-  constexpr int bytes = S::kSmemBytes > floor_bytes ? S::kSmemBytes : floor_bytes;
-  static_assert(bytes <= 227 * 1024, "shared memory of one CTA");
-  UK(cudaFuncSetAttribute(k_conv_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  const int64_t blocks = (a.g.n() + kTcRows - 1) / kTcRows;
-  k_conv_tc<CI, CO><<<(unsigned)blocks, kTcThreads, bytes, net->stream>>>(a);
+  constexpr int kMax = 227 * 1024;
+  if constexpr (ConvTc2Shape<CI, CO>::kSmemBytes <= kMax) {
+    constexpr int need = ConvTc2Shape<CI, CO>::kSmemBytes;
+    constexpr int bytes = need > floor_bytes ? need : floor_bytes;
+    UK(cudaFuncSetAttribute(k_conv_tc2<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    const int64_t blocks = (int64_t)((a.g.nx + 7) / 8) * ((a.g.ny + 15) / 16) * a.g.nz;
+    k_conv_tc2<CI, CO><<<(unsigned)blocks, kTcThreads, bytes, net->stream>>>(a);
+  } else {
+    constexpr int need = ConvTcShape<CI, CO>::kSmemBytes;
+    constexpr int bytes = need > floor_bytes ? need : floor_bytes;
+    static_assert(bytes <= kMax, "shared memory of one CTA");
+    UK(cudaFuncSetAttribute(k_conv_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    const int64_t blocks = (a.g.n() + kTcRows - 1) / kTcRows;
+    k_conv_tc<CI, CO><<<(unsigned)blocks, kTcThreads, bytes, net->stream>>>(a);
+  }
   UK(cudaGetLastError());
   return PLSQR_OK;
 }
@@ -217,6 +208,45 @@ int check_flag(plsqr_unet *net) {
   return PLSQR_OK;
 }
 
+template <int N>
+int gemm_tc_run(plsqr_unet *net, const GemmTcArgs &a, int mtiles, int splits) {
+  constexpr uint32_t cols = tc_cols(N);
+  constexpr int floor_bytes = cols >= 128 ? 58 * 1024 : cols >= 64 ? 30 * 1024 : 0;
+  constexpr int need = GemmTcShape<N>::kSmemBytes;
+  constexpr int bytes = need > floor_bytes ? need : floor_bytes;
+  static_assert(bytes <= 227 * 1024, "shared memory of one CTA");
+  UK(cudaFuncSetAttribute(k_gemm_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  k_gemm_tc<N><<<dim3((unsigned)mtiles, (unsigned)splits), kTcThreads, bytes, net->stream>>>(a);
+  UK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
+// gw[n][m] = sum_k A[m][k] B[n][k] (A [M][K], B [N][K], BF16) on the
+// tensor cores, split over k so that about two CTAs per SM run.
+int gemm_tc(plsqr_unet *net, const bf16 *A, const bf16 *B, int64_t M, int64_t K, int N,
+            float *gw) {
+  const int mtiles = (int)((M + kTcRows - 1) / kTcRows);
+  int64_t splits = std::max<int64_t>(1, std::min<int64_t>((K + 63) / 64, 304 / mtiles));
+  while (splits > 1 && splits * M * N > net->part_cap) --splits;
+  int64_t kchunk = (K + splits - 1) / splits;
+  kchunk = (kchunk + 63) / 64 * 64;
+  splits = (K + kchunk - 1) / kchunk;
+  if (splits * M * N > net->part_cap) {
+    snprintf(net->err, sizeof net->err, "weight-gradient scratch too small");
+    return PLSQR_ERR_ARG;
+  }
+  GemmTcArgs a{A, B, M, K, kchunk, net->part, net->dflag};
+  int rc = PLSQR_ERR_ARG;
+  if (N == 16) rc = gemm_tc_run<16>(net, a, mtiles, (int)splits);
+  else if (N == 32) rc = gemm_tc_run<32>(net, a, mtiles, (int)splits);
+  else if (N == 64) rc = gemm_tc_run<64>(net, a, mtiles, (int)splits);
+  else snprintf(net->err, sizeof net->err, "no tensor-core weight gradient for %d channels", N);
+  if (rc) return rc;
+  k_gemm_tc_reduce<<<grid_for(M * N), kT, 0, net->stream>>>(net->part, (int)splits, M, N, gw);
+  UK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
 // act = relu(conv(x) + b): one implicit-GEMM launch.
 int conv_fwd(plsqr_unet *net, Conv &L, const bf16 *x, bf16 *act) {
   ConvTcArgs a{};
@@ -241,17 +271,15 @@ int conv_bwd(plsqr_unet *net, Conv &L, const bf16 *x, const bf16 *act, const flo
   const int64_t n = L.g.n(), K = L.K();
   int rc;
   k_relu_back<<<grid_for(n * L.cout), kT, 0, s>>>(dact, act, n * L.cout, net->dz);
-  k_bias_grad<<<L.cout, kT, 0, s>>>(net->dz, n, L.cout, L.gb);
-  k_im2col<<<grid_for(n * 27 * (L.cin / 8)), kT, 0, s>>>(x, L.g, L.cin, net->col);
+  k_bias_grad<<<kBiasBlocks, kBiasThreads, 0, s>>>(net->dz, n, L.cout, net->bparts);
+  k_bias_grad_final<<<1, 128, 0, s>>>(net->bparts, kBiasBlocks, L.cout, L.gb);
+  k_im2col_t<<<grid_for(27 * n / 2), kT, 0, s>>>(x, L.g, L.cin, net->colt);
   const dim3 tb(32, 8);
   k_transpose_bf16<<<dim3((unsigned)((L.cout + 31) / 32), (unsigned)((n + 31) / 32)), tb, 0, s>>>(
       net->dz, n, L.cout, net->dzt);
-  k_transpose_bf16<<<dim3((unsigned)((K + 31) / 32), (unsigned)((n + 31) / 32)), tb, 0, s>>>(
-      net->col, n, K, net->colt);
   UK(cudaGetLastError());
-  // dW[co][k] = sum_p dz[p][co] col[p][k]
-  const int splits = (int)std::min<int64_t>(64, std::max<int64_t>(1, n / 4096));
-  if ((rc = gemm(net, net->dzt, n, net->colt, n, L.gw, L.cout, K, n, splits))) return rc;
+  // dW[co][k] = sum_p dz[p][co] colt[k][p]
+  if ((rc = gemm_tc(net, net->colt, net->dzt, K, n, L.cout, L.gw))) return rc;
   if (dx) {
     // dx[p][ci] = sum_t sum_co dz[p - offset(t)][co] W[co][t*cin + ci]: the
     // implicit GEMM on dz with mirrored taps and B_t[ci][co] = wbt[t*cin + ci][co]
@@ -394,10 +422,11 @@ namespace {
 // entries, n * cout outputs and cout x K weights.
 int alloc_scratch(plsqr_unet *net, int64_t max_nk, int64_t max_ncout, int64_t max_wk) {
   int rc;
-  if ((rc = nalloc(net, &net->col, max_nk)) || (rc = nalloc(net, &net->colt, max_nk)) ||
+  if ((rc = nalloc(net, &net->colt, max_nk)) || (rc = nalloc(net, &net->bparts, kBiasBlocks * 128)) ||
       (rc = nalloc(net, &net->dz, max_ncout)) || (rc = nalloc(net, &net->dzt, max_ncout)) ||
       (rc = nalloc(net, &net->part, 64 * max_wk)) || (rc = nalloc(net, &net->dflag, 1)))
     return rc;
+  net->part_cap = 64 * max_wk;
   return PLSQR_OK;
 }
 

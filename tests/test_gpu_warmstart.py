@@ -48,7 +48,7 @@ def col2im(dcol, grid, cin):
     return out[1:-1, 1:-1, 1:-1].reshape(n, cin)
 
 
-@pytest.mark.parametrize("cin,cout", [(16, 32), (48, 16), (32, 64)])
+@pytest.mark.parametrize("cin,cout", [(16, 32), (48, 16), (32, 64), (64, 64), (96, 32)])
 def test_conv_layer_matches_numpy(pkg, cin, cout):
     grid = (8, 6, 4)
     n = 8 * 6 * 4
