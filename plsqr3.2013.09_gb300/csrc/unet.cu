@@ -1,11 +1,11 @@
 // The warm-start network: a 3-D U-Net (3 levels, 16/32/64 channels) from the
 // column-norm-scaled back-projection A^T b to a starting solution x0 on the
 // model grid, trained on (A^T b, x_LSQR) pairs that this library's solvers
-// produce.  Weights are FP32 masters with BF16 copies.  The forward
-// convolutions and their input gradients are implicit GEMMs on the tcgen05
-// tensor cores (BF16 operands, FP32 accumulation in tensor memory,
-// conv_tc.cuh); the weight gradients are im2col + BF16 mma.sync GEMMs
-// (nn_kernels.cuh).  One volume per step, Adam.
+// produce.  Weights are FP32 masters with BF16 copies.  Every contraction
+// runs on the tcgen05 tensor cores (BF16 operands, FP32 accumulation in
+// tensor memory, conv_tc.cuh): the forward convolutions and their input
+// gradients as implicit GEMMs, the weight gradients as a split-K GEMM on the
+// transposed im2col block (nn_kernels.cuh).  One volume per step, Adam.
 //
 //   x16 = input / s (channel 0 of 16)                          level 0
 //   e1 = relu(conv(relu(conv(x16, 16)), 16))                   level 0
