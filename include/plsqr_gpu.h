@@ -371,6 +371,13 @@ int plsqr_unet_predict(plsqr_unet *net, const float *in, float *out);
  * the mean squared error in units of the input's root mean square. */
 int plsqr_unet_train_step(plsqr_unet *net, const float *in, const float *target, float lr,
                           float *loss);
+/* The same two calls on device arrays (nx*ny*nz floats on the network's
+ * device), ordered after the work already queued on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream); the caller's stream
+ * waits for the result.  Both return once the step has run. */
+int plsqr_unet_predict_device(plsqr_unet *net, const float *in, float *out, void *stream);
+int plsqr_unet_train_step_device(plsqr_unet *net, const float *in, const float *target, float lr,
+                                 float *loss, void *stream);
 /* All weights (set = 0: read into buf; 1: load from buf).  buf = NULL:
  * *count = the number of floats. */
 int plsqr_unet_weights(plsqr_unet *net, float *buf, int64_t *count, int32_t set);

@@ -134,6 +134,8 @@ SIGNATURES = {
     "plsqr_unet_last_error": (C.c_char_p, [vp]),
     "plsqr_unet_predict": (C.c_int, [vp, vp, vp]),
     "plsqr_unet_train_step": (C.c_int, [vp, vp, vp, C.c_float, C.POINTER(C.c_float)]),
+    "plsqr_unet_predict_device": (C.c_int, [vp, vp, vp, vp]),
+    "plsqr_unet_train_step_device": (C.c_int, [vp, vp, vp, C.c_float, C.POINTER(C.c_float), vp]),
     "plsqr_unet_weights": (C.c_int, [vp, vp, C.POINTER(i64), i32]),
     "plsqr_nn_conv3d_check": (C.c_int, [i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
     "plsqr_default_problem": (None, [C.POINTER(ProblemDesc)]),

@@ -212,6 +212,23 @@ __global__ void k_take_channels(const float *__restrict__ src, int64_t n, int C,
   }
 }
 
+// Per-block sums of squares of the input volume (FP64, fixed order), for its
+// root mean square.
+__global__ void k_sumsq_in(const float *__restrict__ in, int64_t n, double *__restrict__ parts) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += (double)in[i] * in[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) parts[blockIdx.x] = red[0];
+}
+
 // The input volume (scaled by 1/s) into channel 0 of a 16-channel block.
 __global__ void k_input16(const float *__restrict__ in, int64_t n, float inv_s,
                           __nv_bfloat16 *__restrict__ out) {

@@ -77,6 +77,8 @@ struct plsqr_unet {
   float *part = nullptr, *in = nullptr, *out = nullptr, *target = nullptr, *hparts = nullptr,
         *bparts = nullptr;
   unsigned int *dflag = nullptr;  // set by a tensor-core kernel whose wait ran out
+  double *sparts = nullptr;       // per-block sums of squares of the input
+  cudaEvent_t ev = nullptr;       // orders the device-array calls with the caller's stream
   int64_t part_cap = 0;           // floats of part
   int64_t step = 0;
   char err[256] = {0};
@@ -407,11 +409,22 @@ int backward(plsqr_unet *net, float s, float lr, float *loss) {
   return PLSQR_OK;
 }
 
-float rms_of(const float *v, int64_t n) {
-  double s = 0.0;
-  for (int64_t i = 0; i < n; ++i) s += (double)v[i] * v[i];
-  const double r = n > 0 ? sqrt(s / (double)n) : 0.0;
-  return r > 0.0 ? (float)r : 1.f;
+constexpr int kRmsBlocks = 304;
+
+// The root mean square of net->in (1 for a zero volume): FP64 block sums on
+// the device, added in block order on the host.
+int input_rms(plsqr_unet *net, float *s) {
+  const int64_t n = net->g0.n();
+  k_sumsq_in<<<kRmsBlocks, 256, 0, net->stream>>>(net->in, n, net->sparts);
+  UK(cudaGetLastError());
+  double h[kRmsBlocks];
+  UK(cudaMemcpyAsync(h, net->sparts, sizeof h, cudaMemcpyDeviceToHost, net->stream));
+  UK(cudaStreamSynchronize(net->stream));
+  double t = 0.0;
+  for (int b = 0; b < kRmsBlocks; ++b) t += h[b];
+  const double r = n > 0 ? sqrt(t / (double)n) : 0.0;
+  *s = r > 0.0 ? (float)r : 1.f;
+  return PLSQR_OK;
 }
 
 }  // namespace
@@ -434,6 +447,7 @@ void free_net(plsqr_unet *net) {
   if (!net) return;
   cudaSetDevice(net->device);
   for (void *p : net->allocs) cudaFree(p);
+  if (net->ev) cudaEventDestroy(net->ev);
   if (net->stream) cudaStreamDestroy(net->stream);
   delete net;
 }
@@ -479,8 +493,9 @@ int build_net(plsqr_unet *net, uint64_t seed) {
       (rc = nalloc(net, &net->out, n0)) || (rc = nalloc(net, &net->target, n0)) ||
       (rc = nalloc(net, &net->hparts, 152 * 4 * 18)) || (rc = nalloc(net, &net->hw, 17)) ||
       (rc = nalloc(net, &net->hm, 17)) || (rc = nalloc(net, &net->hv, 17)) ||
-      (rc = nalloc(net, &net->hg, 17)))
+      (rc = nalloc(net, &net->hg, 17)) || (rc = nalloc(net, &net->sparts, kRmsBlocks)))
     return rc;
+  UK(cudaEventCreateWithFlags(&net->ev, cudaEventDisableTiming));
   float h[17];
   for (int c = 0; c < 16; ++c) h[c] = (float)(0.25 * det_normal(seed + 77, (uint64_t)c));
   h[16] = 0.f;
@@ -525,14 +540,43 @@ extern "C" void plsqr_unet_destroy(plsqr_unet *net) { free_net(net); }
 
 extern "C" const char *plsqr_unet_last_error(const plsqr_unet *net) { return net ? net->err : ""; }
 
-extern "C" int plsqr_unet_predict(plsqr_unet *net, const float *in, float *out) {
-  if (!net || !in || !out) return PLSQR_ERR_ARG;
+// The calls on host arrays (kind = cudaMemcpyHostToDevice / DeviceToHost)
+// and on device arrays ordered on the caller's stream (DeviceToDevice).
+static int predict_impl(plsqr_unet *net, const float *in, float *out, cudaMemcpyKind kin,
+                        cudaMemcpyKind kout) {
   const int64_t n = net->g0.n();
   UK(cudaSetDevice(net->device));
-  UK(cudaMemcpyAsync(net->in, in, sizeof(float) * n, cudaMemcpyHostToDevice, net->stream));
+  UK(cudaMemcpyAsync(net->in, in, sizeof(float) * n, kin, net->stream));
+  float s = 1.f;
   int rc;
-  if ((rc = forward(net, rms_of(in, n)))) return rc;
-  UK(cudaMemcpyAsync(out, net->out, sizeof(float) * n, cudaMemcpyDeviceToHost, net->stream));
+  if ((rc = input_rms(net, &s)) || (rc = forward(net, s))) return rc;
+  UK(cudaMemcpyAsync(out, net->out, sizeof(float) * n, kout, net->stream));
+  return PLSQR_OK;
+}
+
+static int train_impl(plsqr_unet *net, const float *in, const float *target, float lr,
+                      float *loss, cudaMemcpyKind kin) {
+  const int64_t n = net->g0.n();
+  UK(cudaSetDevice(net->device));
+  UK(cudaMemcpyAsync(net->in, in, sizeof(float) * n, kin, net->stream));
+  UK(cudaMemcpyAsync(net->target, target, sizeof(float) * n, kin, net->stream));
+  float s = 1.f;
+  int rc;
+  if ((rc = input_rms(net, &s)) || (rc = forward(net, s))) return rc;
+  return backward(net, s, lr, loss);
+}
+
+// Make the network's stream wait for `from`.
+static int stream_after(plsqr_unet *net, cudaStream_t to, cudaStream_t from) {
+  UK(cudaEventRecord(net->ev, from));
+  UK(cudaStreamWaitEvent(to, net->ev, 0));
+  return PLSQR_OK;
+}
+
+extern "C" int plsqr_unet_predict(plsqr_unet *net, const float *in, float *out) {
+  if (!net || !in || !out) return PLSQR_ERR_ARG;
+  int rc;
+  if ((rc = predict_impl(net, in, out, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost))) return rc;
   UK(cudaStreamSynchronize(net->stream));
   return PLSQR_OK;
 }
@@ -540,14 +584,33 @@ extern "C" int plsqr_unet_predict(plsqr_unet *net, const float *in, float *out) 
 extern "C" int plsqr_unet_train_step(plsqr_unet *net, const float *in, const float *target,
                                      float lr, float *loss) {
   if (!net || !in || !target || !(lr > 0.f)) return PLSQR_ERR_ARG;
-  const int64_t n = net->g0.n();
+  return train_impl(net, in, target, lr, loss, cudaMemcpyHostToDevice);
+}
+
+extern "C" int plsqr_unet_predict_device(plsqr_unet *net, const float *in, float *out,
+                                         void *stream) {
+  if (!net || !in || !out) return PLSQR_ERR_ARG;
+  const cudaStream_t cs = (cudaStream_t)stream;
   UK(cudaSetDevice(net->device));
-  UK(cudaMemcpyAsync(net->in, in, sizeof(float) * n, cudaMemcpyHostToDevice, net->stream));
-  UK(cudaMemcpyAsync(net->target, target, sizeof(float) * n, cudaMemcpyHostToDevice, net->stream));
-  const float s = rms_of(in, n);
   int rc;
-  if ((rc = forward(net, s))) return rc;
-  return backward(net, s, lr, loss);
+  if ((rc = stream_after(net, net->stream, cs)) ||
+      (rc = predict_impl(net, in, out, cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice)) ||
+      (rc = stream_after(net, cs, net->stream)))
+    return rc;
+  return PLSQR_OK;
+}
+
+extern "C" int plsqr_unet_train_step_device(plsqr_unet *net, const float *in, const float *target,
+                                            float lr, float *loss, void *stream) {
+  if (!net || !in || !target || !(lr > 0.f)) return PLSQR_ERR_ARG;
+  const cudaStream_t cs = (cudaStream_t)stream;
+  UK(cudaSetDevice(net->device));
+  int rc;
+  if ((rc = stream_after(net, net->stream, cs)) ||
+      (rc = train_impl(net, in, target, lr, loss, cudaMemcpyDeviceToDevice)) ||
+      (rc = stream_after(net, cs, net->stream)))
+    return rc;
+  return PLSQR_OK;
 }
 
 // All trainable values, layer by layer (w then b), then the head (16 + 1).

@@ -61,6 +61,11 @@ class UNet:
                                                   C.byref(loss)), "plsqr_unet_train_step")
         return float(loss.value)
 
+    @property
+    def handle(self) -> int:
+        """The plsqr_unet pointer, for the PyTorch custom ops (torch_ops)."""
+        return int(self._h.value)
+
     def weights(self) -> np.ndarray:
         cnt = N.i64(0)
         self._check(N.lib().plsqr_unet_weights(self._h, None, C.byref(cnt), 0), "plsqr_unet_weights")
@@ -74,6 +79,62 @@ class UNet:
         cnt = N.i64(b.size)
         self._check(N.lib().plsqr_unet_weights(self._h, N.ptr(b), C.byref(cnt), 1),
                     "plsqr_unet_weights")
+
+
+_OPS = None
+
+
+def torch_ops():
+    """The network as PyTorch custom ops on CUDA tensors (registered once):
+    torch.ops.plsqr.unet_predict(net, z) -> x0 and
+    torch.ops.plsqr.unet_train_step(net, z, target, lr) -> loss (a 0-d CPU
+    tensor), with net = UNet.handle and float32 volumes of the network's
+    grid on its device.  They run the device-array calls
+    (plsqr_unet_*_device) ordered on the current CUDA stream."""
+    global _OPS
+    if _OPS is not None:
+        return _OPS
+    import torch
+
+    def _vol(t, name: str):
+        if t.dtype != torch.float32 or not t.is_cuda:
+            raise ValueError(f"{name} must be a float32 CUDA tensor")
+        return t.contiguous()
+
+    @torch.library.custom_op("plsqr::unet_predict", mutates_args=(),
+                             schema="(int net, Tensor z) -> Tensor")
+    def unet_predict(net, z):
+        z = _vol(z, "z")
+        out = torch.empty_like(z)
+        stream = torch.cuda.current_stream(z.device).cuda_stream
+        N.check(N.lib().plsqr_unet_predict_device(C.c_void_p(net), C.c_void_p(z.data_ptr()),
+                                                   C.c_void_p(out.data_ptr()),
+                                                   C.c_void_p(stream)),
+                "plsqr_unet_predict_device")
+        return out
+
+    @unet_predict.register_fake
+    def _(net, z):
+        return torch.empty_like(z)
+
+    @torch.library.custom_op("plsqr::unet_train_step", mutates_args=(),
+                             schema="(int net, Tensor z, Tensor target, float lr) -> Tensor")
+    def unet_train_step(net, z, target, lr):
+        z, target = _vol(z, "z"), _vol(target, "target")
+        loss = C.c_float(0.0)
+        stream = torch.cuda.current_stream(z.device).cuda_stream
+        N.check(N.lib().plsqr_unet_train_step_device(C.c_void_p(net), C.c_void_p(z.data_ptr()),
+                                                      C.c_void_p(target.data_ptr()), float(lr),
+                                                      C.byref(loss), C.c_void_p(stream)),
+                "plsqr_unet_train_step_device")
+        return torch.tensor(loss.value, dtype=torch.float32)
+
+    @unet_train_step.register_fake
+    def _(net, z, target, lr):
+        return torch.empty((), dtype=torch.float32)
+
+    _OPS = torch.ops.plsqr
+    return _OPS
 
 
 def conv3d_check(grid, x, w, b, dy):

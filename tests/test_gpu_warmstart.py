@@ -87,3 +87,28 @@ def test_training_lowers_the_loss_and_is_repeatable(pkg):
     assert all(np.isfinite(losses))
     assert np.mean(losses[-5:]) < 0.5 * np.mean(losses[:5])
     assert rel(p1, target) < rel(p0, target)
+
+
+def test_torch_custom_ops_match_the_host_calls(pkg):
+    """torch.ops.plsqr.unet_predict / unet_train_step on CUDA tensors give the
+    bits of plsqr_unet_predict / plsqr_unet_train_step on host arrays."""
+    torch = pytest.importorskip("torch")
+    grid = (16, 16, 8)
+    n = 16 * 16 * 8
+    rng = np.random.default_rng(11)
+    z = rng.standard_normal(n).astype(np.float32)
+    target = (0.5 * z + 0.2 * np.roll(z, 1)).astype(np.float32)
+    ops = pkg.warm.torch_ops()
+    zt = torch.tensor(z, device="cuda")
+    tt = torch.tensor(target, device="cuda")
+    with pkg.warm.UNet(grid, seed=4) as a, pkg.warm.UNet(grid, seed=4) as b:
+        p_host = a.predict(z)
+        p_dev = ops.unet_predict(b.handle, zt)
+        assert np.array_equal(p_host, p_dev.cpu().numpy().astype(np.float64))
+        for lr in (2e-3, 1e-3):
+            l_host = a.train_step(z, target, lr)
+            l_dev = ops.unet_train_step(b.handle, zt, tt, lr)
+            assert l_host == float(l_dev)
+        assert np.array_equal(a.weights(), b.weights())
+        assert np.array_equal(a.predict(z), ops.unet_predict(b.handle, zt).cpu().numpy()
+                              .astype(np.float64))

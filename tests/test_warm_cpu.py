@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import numpy as np
+import pytest
 
 
 def test_model_instances_are_seeded(pkg):
@@ -23,3 +24,11 @@ def test_column_norms(pkg):
             v = L.val[L.ptr[c]:L.ptr[c + 1]]
             ref[c] += v @ v
     assert np.allclose(cn, ref, rtol=1e-14, atol=0)
+
+
+def test_torch_ops_register_and_check_their_tensors(pkg):
+    torch = pytest.importorskip("torch")
+    ops = pkg.warm.torch_ops()
+    assert pkg.warm.torch_ops() is ops
+    with pytest.raises(ValueError):
+        ops.unet_predict(0, torch.zeros(8))
