@@ -82,7 +82,10 @@ int mixed_prepare(plsqr_ctx *ctx) {
     int slab = 24576;  // 96 KB of FP32 per block: two blocks per SM
     if (const char *e = getenv("PLSQR_SLAB_SIZE_F"))
       if (atoi(e) >= 1024 && atoi(e) <= 57344) slab = atoi(e);
-    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &M->s_rows)) ||
+    // kernel rows: mostly consecutive columns, read by the lanes of a
+    // group in step (transposed chunks); columns: random rows, as stored
+    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &M->s_rows,
+                                ctx->slab_group_f)) ||
         (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &M->s_cols)))
       return rc;
     if ((rc = slab_set_smem<float>(std::max(M->s_rows.smem, M->s_cols.smem)))) return rc;

@@ -77,8 +77,10 @@ struct plsqr_ctx {
 
 // slab.cu
 template <typename T>
+// tgroup > 1: transpose each segment's chunks for products that stream it
+// with tgroup lanes (slab_pos in slab.cuh); 0 keeps the order
 int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, int blocks,
-               DevSlab<T> *out);
+               DevSlab<T> *out, int tgroup = 0);
 int slab_plan(plsqr_ctx *ctx);
 // plsqr_gpu.cu: slab product launch and its shared-memory attribute
 template <typename T>

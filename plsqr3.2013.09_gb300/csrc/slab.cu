@@ -28,7 +28,7 @@ constexpr int kMaxSlabs = 64;  // k_slab_count / k_slab_fill keep one counter pe
 
 template <typename T>
 int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, int blocks,
-               DevSlab<T> *out) {
+               DevSlab<T> *out, int tgroup) {
   const int n_lines = L.n_lines;
   const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
   if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
@@ -64,7 +64,7 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, i
     return rc;
   CK(cudaMemcpy(out->ptr, sp.data(), sizeof(int64_t) * sp.size(), cudaMemcpyHostToDevice));
   k_slab_fill<T><<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, L.val, n_lines, n_slabs, slab, out->ptr,
-                                             out->idx, out->val);
+                                             tgroup, out->idx, out->val);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   // blocks per slab: `blocks` in total (several waves of small, nonzero-
@@ -108,9 +108,9 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, i
 }
 
 template int build_slab<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t, int,
-                                DevSlab<double> *);
+                                DevSlab<double> *, int);
 template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, int,
-                               DevSlab<float> *);
+                               DevSlab<float> *, int);
 
 // Plan the slab paths.  slab_ok: every dimension fits kMaxSlabs slabs of
 // 24,576 FP32 values, so the mixed solver's inner products use FP32 slabs.

@@ -49,26 +49,44 @@ static __global__ void k_slab_count(const int64_t *__restrict__ ptr, const int32
   }
 }
 
+// Stored position of the segment's entry o (segment length len, a multiple
+// of 8) when a product streams the segment with tgroup lanes: each chunk of
+// tgroup groups of 8 (ng groups in a shorter last chunk) is transposed so
+// that lane l's group holds the chunk's entries l, l + ng, l + 2 ng, ....
+// At every step of the product the group's lanes then read consecutive
+// entries: for a kernel row, mostly consecutive columns, which fall in
+// distinct shared-memory banks.  tgroup <= 1 keeps the order.
+__host__ __device__ __forceinline__ int64_t slab_pos(int64_t o, int64_t len, int tgroup) {
+  if (tgroup <= 1) return o;
+  const int64_t cw = (int64_t)tgroup * 8, c0 = (o / cw) * cw;
+  const int64_t ng = (len - c0) / 8 < tgroup ? (len - c0) / 8 : tgroup;
+  const int64_t w = o - c0;
+  return c0 + (w % ng) * 8 + w / ng;
+}
+
 // Scatter line l's entries into its segments; pad with (index 0, value 0).
 template <typename T>
 __global__ void k_slab_fill(const int64_t *__restrict__ ptr, const int32_t *__restrict__ idx,
                             const double *__restrict__ val, int n_lines, int n_slabs, int slab,
-                            const int64_t *__restrict__ sptr, uint16_t *__restrict__ sidx,
-                            T *__restrict__ sval) {
+                            const int64_t *__restrict__ sptr, int tgroup,
+                            uint16_t *__restrict__ sidx, T *__restrict__ sval) {
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n_lines; l += gridDim.x * blockDim.x) {
     int64_t cur[64];
-    for (int s = 0; s < n_slabs; ++s) cur[s] = sptr[(int64_t)s * (n_lines + 1) + l];
+    for (int s = 0; s < n_slabs; ++s) cur[s] = 0;
     for (int64_t e = ptr[l]; e < ptr[l + 1]; ++e) {
       const int s = idx[e] / slab;
-      const int64_t o = cur[s]++;
+      const int64_t b = sptr[(int64_t)s * (n_lines + 1) + l];
+      const int64_t o = b + slab_pos(cur[s]++, sptr[(int64_t)s * (n_lines + 1) + l + 1] - b, tgroup);
       sidx[o] = (uint16_t)(idx[e] - s * slab);
       sval[o] = (T)val[e];
     }
     for (int s = 0; s < n_slabs; ++s) {
-      const int64_t end = sptr[(int64_t)s * (n_lines + 1) + l + 1];
-      for (int64_t o = cur[s]; o < end; ++o) {
-        sidx[o] = 0;
-        sval[o] = (T)0;
+      const int64_t b = sptr[(int64_t)s * (n_lines + 1) + l];
+      const int64_t len = sptr[(int64_t)s * (n_lines + 1) + l + 1] - b;
+      for (int64_t o = cur[s]; o < len; ++o) {
+        const int64_t q = b + slab_pos(o, len, tgroup);
+        sidx[q] = 0;
+        sval[q] = (T)0;
       }
     }
   }
