@@ -1,0 +1,72 @@
+"""The tuning switches (environment variables read when a context is
+created) select other layouts and launch shapes of the same products; each
+one must keep the FP64 solve within 1e-10 of the reference's golden run and
+the mixed solve within 1e-6 of the FP64 solution."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel
+
+pytestmark = pytest.mark.gpu
+
+LSQR_TOL = 1e-10
+
+
+def per_iter_rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+FP64_CASES = [
+    {"PLSQR_SLABS": "0"},                                   # per-line A^T y (k_aprod2)
+    {"PLSQR_SLABS": "0", "PLSQR_M2_BLOCKS_PER_SM": "3"},
+    {"PLSQR_SLABS": "1"},                                   # FP64 row slabs for A x too
+    {"PLSQR_SLAB_SIZE": "1024"},                            # many slabs, short segments
+    {"PLSQR_SLABS": "1", "PLSQR_SLAB_SIZE": "1024"},
+    {"PLSQR_SLAB_GROUP": "4"},
+    {"PLSQR_SLAB_GROUP": "16"},
+    {"PLSQR_SLAB_GROUP": "32"},
+    {"PLSQR_SLAB_BLOCKS": "7"},
+    {"PLSQR_UNROLL": "1"},
+    {"PLSQR_UNROLL": "4"},
+    {"PLSQR_BLOCKS_PER_SM": "1"},
+    {"PLSQR_NATURAL_ORDER": "1", "PLSQR_SLABS": "0"},
+]
+
+
+@pytest.mark.parametrize("env", FP64_CASES, ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
+def test_fp64_switches_match_reference(env, pkg, problems, monkeypatch):
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    g = golden("grid32")
+    prob = problems("grid32")
+    it = g["meta"]["iterations"]
+    with pkg.Context(prob) as ctx:
+        out = ctx.lsqr(lsqr_iteration=it)
+    assert rel(out["x"], g["x"]) <= LSQR_TOL
+    assert per_iter_rel(out["hist"]["alpha"], g["alpha"]) <= LSQR_TOL
+    assert per_iter_rel(out["hist"]["beta"], g["beta"]) <= LSQR_TOL
+
+
+MIXED_CASES = [
+    {"PLSQR_MIXED_F32VEC": "1"},                            # FP32 vectors in the inner sweeps
+    {"PLSQR_SLAB_SIZE_F": "1024"},
+    {"PLSQR_SLAB_GROUP_F": "4"},                            # transposed chunks of other widths
+    {"PLSQR_SLAB_GROUP_F": "8"},
+    {"PLSQR_SLAB_GROUP_F": "32"},
+    {"PLSQR_SLABS": "0"},
+]
+
+
+@pytest.mark.parametrize("env", MIXED_CASES, ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
+def test_mixed_switches_reach_the_fp64_solution(env, pkg, problems, monkeypatch):
+    prob = problems("grid32")
+    with pkg.Context(prob) as c64:
+        xstar = c64.lsqr(lsqr_iteration=400)["x"]
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    with pkg.Context(prob, precision="mixed") as cm:
+        out = cm.lsqr(sweeps=5, inner=60)
+    assert rel(out["x"], xstar) <= 1e-6
