@@ -19,6 +19,13 @@ precision, clocks sampled during the timed region.
 `--impl reference` times the reference CPU implementation of the same solve
 (the oracle port of source/lsqr.c + aprod_impl.c + CPUSpMV.c, OpenMP on all
 host cores) on a bounded sample and prints the same metric.
+
+`--extension batched|uneven|warm` measures an extension instead (one JSON
+line each): 32 right-hand sides on the 96x96x32 operator against the plain
+path run once per right-hand side; the 24 uneven problems in one persistent
+launch against the one-problem path; the learned warm start (2,000 training
+pairs, training, iterations and time to 1e-6 on held-out seeds, cold
+against warm).  `--profile` runs one short case of the chosen path for ncu.
 """
 from __future__ import annotations
 
@@ -181,7 +188,8 @@ def main() -> int:
                     help="warm start: held-out seeds timed to 1e-6 against FP64 references")
     ap.add_argument("--extension", default=None, choices=["batched", "uneven", "warm"],
                     help="measure an extension instead: 32 right-hand sides on the "
-                         "96x96x32 operator, or the 24 uneven problems in one launch")
+                         "96x96x32 operator, the 24 uneven problems in one launch, or the "
+                         "learned warm start (training set, training, held-out iterations)")
     ap.add_argument("--variant-rows", type=int, default=-1,
                     help="batched product variant of A x (-1: pick by timing)")
     ap.add_argument("--variant-cols", type=int, default=-1,
