@@ -93,7 +93,7 @@ __global__ void k_relu_back(const float *__restrict__ d, const __nv_bfloat16 *__
 // of kBiasThreads threads reads a grid-strided share of dz in storage order
 // (a thread keeps one channel, as kBiasThreads * gridDim is a multiple of
 // C) and writes its per-channel sums to parts[block][C]; k_bias_grad_final
-// adds the blocks' sums in block order.
+// (one warp per channel) adds the blocks' sums in a fixed order.
 constexpr int kBiasThreads = 192;  // a multiple of 16, 32, 48, 64 and 96
 
 __global__ void __launch_bounds__(kBiasThreads)
@@ -115,11 +115,12 @@ __global__ void __launch_bounds__(kBiasThreads)
 
 __global__ void k_bias_grad_final(const float *__restrict__ parts, int blocks, int C,
                                   float *__restrict__ db) {
-  const int c = threadIdx.x;
-  if (c >= C) return;
+  const int c = blockIdx.x, lane = threadIdx.x;
   float t = 0.f;
-  for (int b = 0; b < blocks; ++b) t += parts[(int64_t)b * C + c];
-  db[c] = t;
+  for (int b = lane; b < blocks; b += 32) t += parts[(int64_t)b * C + c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) db[c] = t;
 }
 
 // 2x2x2 average pooling of a channels-last block (fine grid g).

@@ -274,7 +274,7 @@ int conv_bwd(plsqr_unet *net, Conv &L, const bf16 *x, const bf16 *act, const flo
   int rc;
   k_relu_back<<<grid_for(n * L.cout), kT, 0, s>>>(dact, act, n * L.cout, net->dz);
   k_bias_grad<<<kBiasBlocks, kBiasThreads, 0, s>>>(net->dz, n, L.cout, net->bparts);
-  k_bias_grad_final<<<1, 128, 0, s>>>(net->bparts, kBiasBlocks, L.cout, L.gb);
+  k_bias_grad_final<<<L.cout, 32, 0, s>>>(net->bparts, kBiasBlocks, L.cout, L.gb);
   k_im2col_t<<<grid_for(27 * n / 2), kT, 0, s>>>(x, L.g, L.cin, net->colt);
   const dim3 tb(32, 8);
   k_transpose_bf16<<<dim3((unsigned)((L.cout + 31) / 32), (unsigned)((n + 31) / 32)), tb, 0, s>>>(
