@@ -9,7 +9,9 @@
  * p_resultx_itn=<K>_NProc=1_float64_mpiio.bin.  -row_ptn, -col_ptn and
  * -col_perm describe a multi-rank partition and are accepted and ignored.
  * Additional options: -precision fp64|mixed, -sweeps S, -inner I, -device G,
- * -quiet.
+ * -quiet, and -x0 FILE: a starting solution for the mixed solver, col raw
+ * float64 values (the format of the solution file above), kept where it
+ * lowers the residual.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -26,6 +28,7 @@ int main(int argc, char **argv) {
   const char *damp_i_c = "plsqr3_reorder_small_all.damp.bycol.info.bin";
   const char *damp_f_c = "plsqr3_reorder_small_all.damp.bycol.bin";
   const char *b_k = "vecotrB_ker";
+  const char *x0_path = NULL;
   int row_k = 10, row_d = 1825, col = 520, itn = 40;
   int precision = PLSQR_PREC_FP64, sweeps = 4, inner = 50, device = 0, verbose = 1;
   for (int i = 1; i < argc; i++) {
@@ -51,6 +54,7 @@ int main(int argc, char **argv) {
     STR("-damp_i_bycol", damp_i_c);
     STR("-damp_f_bycol", damp_f_c);
     STR("-b_k", b_k);
+    STR("-x0", x0_path);
     INT("-row_k", row_k);
     INT("-row_d", row_d);
     INT("-col", col);
@@ -104,9 +108,25 @@ int main(int argc, char **argv) {
   a.result_txt = "result.txt";
   a.sweeps = sweeps;
   a.inner = inner;
+  double *x0 = NULL;
+  if (x0_path) {
+    FILE *fx = fopen(x0_path, "rb");
+    x0 = (double *)malloc(sizeof(double) * (size_t)(col > 0 ? col : 1));
+    const size_t got = fx && x0 ? fread(x0, sizeof(double), (size_t)col, fx) : 0;
+    if (fx) fclose(fx);
+    if (got != (size_t)col) {
+      fprintf(stderr, "plsqr3_gpu: cannot read %d float64 values from %s\n", col, x0_path);
+      free(x0);
+      plsqr_ctx_destroy(ctx);
+      return 1;
+    }
+    a.x0 = x0;
+  }
   printf("\nStarting plsqr algorithm...procRank=%d\n", 0);
   plsqr_result r;
   rc = plsqr_lsqr(ctx, &a, NULL, NULL, NULL, NULL, NULL, &r);
+  free(x0);
+  if (rc == PLSQR_OK && x0_path) printf("x0 %s\n", r.warm ? "kept" : "not kept (cold start)");
   if (rc) {
     fprintf(stderr, "plsqr3_gpu: lsqr failed: %s (%s)\n", plsqr_strerror(rc),
             plsqr_ctx_last_error(ctx));

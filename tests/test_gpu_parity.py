@@ -268,3 +268,33 @@ def test_mixed_precision_warm_start(pkg, problems):
         with pytest.raises(pkg._native.PlsqrError) as e:
             cm.lsqr(damp=0.1, sweeps=1, inner=10, x0=x0)
         assert e.value.code == -1
+
+
+def test_cli_warm_start_from_a_solution_file(pkg, problems, tmp_path):
+    """-x0 FILE (the program's own float64 solution format) starts the mixed
+    solver from that solution, which it keeps and does not make worse in the
+    least-squares residual; the FP64 path refuses it."""
+    g = golden("tiny")
+    f = g["meta"]["files"]
+    exe = pkg._native.LIB_DIR / "plsqr3_gpu"
+    it = g["meta"]["iterations"]
+    base = [str(exe), "-dir", str(GOLDEN / "tiny" / "inputs"), "-quiet"]
+    for k in ("ker_f", "ker_i", "damp_f", "damp_i", "damp_f_bycol", "damp_i_bycol", "b_k"):
+        base += [f"-{k}", f[k]]
+    base += ["-row_k", str(f["row_k"]), "-row_d", str(f["row_d"]), "-col", str(f["col"]),
+             "-itn", str(it)]
+    out = tmp_path / f"p_resultx_itn={it}_NProc=1_float64_mpiio.bin"
+    subprocess.run(base, cwd=tmp_path, check=True, capture_output=True)
+    x0 = tmp_path / "x0.bin"
+    x0.write_bytes(out.read_bytes())
+    mixed = base + ["-precision", "mixed", "-sweeps", "1", "-inner", "20", "-x0", str(x0)]
+    p = subprocess.run(mixed, cwd=tmp_path, check=True, capture_output=True, text=True)
+    assert "x0 kept" in p.stdout
+    prob = problems("tiny")
+    A = scipy_ops(prob)
+    b = np.concatenate([prob.b_k, np.zeros(prob.m_d)])
+    r0 = np.linalg.norm(b - A @ np.fromfile(x0, dtype=np.float64))
+    r1 = np.linalg.norm(b - A @ np.fromfile(out, dtype=np.float64))
+    assert np.isfinite(r1) and r1 <= r0 * (1 + 1e-9)
+    p = subprocess.run(base + ["-x0", str(x0)], cwd=tmp_path, capture_output=True, text=True)
+    assert p.returncode != 0 and "mixed-precision" in p.stderr
