@@ -40,7 +40,10 @@ extern "C" {
 #define PLSQR_ERR_STATE (-7)    /* call out of sequence                        */
 #define PLSQR_ERR_TIMEOUT (-8)  /* a bounded device wait gave up               */
 #define PLSQR_ERR_INTERNAL (-9) /* internal consistency check failed           */
-#define PLSQR_ERR_NUMERIC (-10) /* NaN or Inf in an input vector               */
+#define PLSQR_ERR_NUMERIC (-10) /* NaN or Inf in an input, or magnitudes the
+                                   FP64 sums of squares of the norms cannot
+                                   hold: a largest |value| above 2^500, or a
+                                   vector whose nonzeros are all below 2^-500 */
 
 /* source/main.h:26-36 precision switch, as a run-time choice */
 #define PLSQR_PREC_FP64 0  /* FP64 values, vectors, reductions              */

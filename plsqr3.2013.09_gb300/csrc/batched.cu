@@ -526,8 +526,16 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
   const int S = a->sweeps, I = a->inner;
   const int64_t total = (int64_t)S * I;
   if (total > (int64_t)1 << 24) return PLSQR_ERR_ARG;
-  CK(cudaSetDevice(ctx->opts.device));
   int rc;
+  for (int j = 0; j < k; ++j)
+    if ((rc = magnitude_ok(a->b_k + (int64_t)j * ctx->m_k, ctx->m_k)) ||
+        (a->x0 && (rc = magnitude_ok(a->x0 + (int64_t)j * ctx->n, ctx->n))) ||
+        (a->x_ref && (rc = magnitude_ok(a->x_ref + (int64_t)j * ctx->n, ctx->n)))) {
+      ctx_set_error(ctx, "right-hand side %d: b_k, x0 or x_ref holds NaN, Inf or magnitudes "
+                         "outside [2^-500, 2^500]", j);
+      return rc;
+    }
+  CK(cudaSetDevice(ctx->opts.device));
   if ((rc = batch_prepare(ctx, kw))) return rc;
   BatchState *B = ctx->batch;
   if (!B->lines_sorted && ((a->variant_rows >= 0 && kVariants[a->variant_rows].lpr == 0) ||

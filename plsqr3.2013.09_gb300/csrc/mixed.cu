@@ -248,6 +248,10 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     if ((int32_t)ctx->b_k.size() != ctx->m_k) return PLSQR_ERR_STATE;
     b = ctx->b_k.data();
   }
+  if ((rc = magnitude_ok(b, ctx->m_k)) || (x0 && (rc = magnitude_ok(x0, ctx->n)))) {
+    ctx_set_error(ctx, "b_k or x0 holds NaN, Inf or magnitudes outside [2^-500, 2^500]");
+    return rc;
+  }
   CK(cudaSetDevice(ctx->opts.device));
   const int S = args->sweeps, I = args->inner;
   const int total = S * I;

@@ -43,6 +43,10 @@
 
 using namespace plsqr;
 
+// plsqr_gpu.cu: PLSQR_ERR_NUMERIC for NaN, Inf, or magnitudes outside the
+// range of the FP64 sums of squares
+int magnitude_ok(const double *p, int64_t n, int allow_small = 0);
+
 namespace {
 
 constexpr int kMT = 256;              // threads per block
@@ -498,7 +502,7 @@ int checked_lines(const plsqr_sparse *a, int32_t rows, int32_t cols, bool by_col
   if (a->nnz > 0 && (!a->idx || !a->val)) return PLSQR_ERR_ARG;
   for (int64_t e = 0; e < a->nnz; ++e)
     if (a->idx[e] < 0 || a->idx[e] >= ni) return PLSQR_ERR_FORMAT;
-  return PLSQR_OK;
+  return magnitude_ok(a->val, a->nnz, 1);
 }
 
 void split_by_nnz(const std::vector<int64_t> &pre, int parts, std::vector<int32_t> &out) {
@@ -647,6 +651,10 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
         (rc = checked_lines(&q.d_csr, m_d, n, false, dr[(size_t)p])) ||
         (rc = checked_lines(&q.d_csc, m_d, n, true, dc[(size_t)p]))) {
       set_error(mp, "problem %d: inconsistent operator", p);
+      return rc;
+    }
+    if ((rc = magnitude_ok(q.b_k, m_k))) {
+      set_error(mp, "problem %d: b_k holds NaN, Inf or magnitudes outside [2^-500, 2^500]", p);
       return rc;
     }
     if (q.d_csc.nnz != q.d_csr.nnz) return PLSQR_ERR_FORMAT;

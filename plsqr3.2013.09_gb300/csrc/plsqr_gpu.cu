@@ -40,7 +40,8 @@ const char *const kErrText[] = {
     "call out of sequence",
     "a bounded device wait gave up",
     "internal consistency check failed",
-    "NaN or Inf in an input vector",
+    "NaN, Inf or out-of-range magnitude in an input (|value| above 2^500, or a vector all below "
+    "2^-500)",
 };
 
 }  // namespace
@@ -85,6 +86,25 @@ void ctx_dev_free(plsqr_ctx *ctx, void *p) {
 // ---------------------------------------------------------------------------
 // host-side validation of a compressed sparse matrix (no device fault can
 // come from a bad index: every index is checked before upload)
+// The norms are plain FP64 sums of squares (the reference's cblas_dnrm2,
+// source/mycblas.c:182-222, rescales as it goes): a vector whose largest
+// magnitude is above 2^500, or nonzero but below 2^-500, would overflow or
+// underflow them, and is refused, as are NaN and Inf.  Matrix values
+// (allow_small = 1) are refused only above 2^500: the products of small
+// values underflow in the reference's sums alike.
+int magnitude_ok(const double *p, int64_t n, int allow_small) {
+  double mx = 0.0;
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(max : mx) reduction(| : bad)
+  for (int64_t i = 0; i < n; ++i) {
+    const double a = fabs(p[i]);
+    if (!(a <= 1.7976931348623157e308)) bad = 1;  // NaN or Inf
+    else if (a > mx) mx = a;
+  }
+  if (bad || mx > 0x1p500 || (!allow_small && mx > 0.0 && mx < 0x1p-500)) return PLSQR_ERR_NUMERIC;
+  return PLSQR_OK;
+}
+
 static int validate_sparse(const plsqr_sparse *a, int32_t rows, int32_t cols, int by_col,
                            std::vector<int64_t> &ptr64) {
   if (!a || (!a->ptr32 && !a->ptr64) || (a->ptr32 && a->ptr64)) return PLSQR_ERR_ARG;
@@ -100,7 +120,8 @@ static int validate_sparse(const plsqr_sparse *a, int32_t rows, int32_t cols, in
 #pragma omp parallel for schedule(static) reduction(| : bad)
   for (int64_t e = 0; e < a->nnz; ++e)
     if (a->idx[e] < 0 || a->idx[e] >= n_idx) bad = 1;
-  return bad ? PLSQR_ERR_FORMAT : PLSQR_OK;
+  if (bad) return PLSQR_ERR_FORMAT;
+  return magnitude_ok(a->val, a->nnz, 1);
 }
 
 static int upload_lines(plsqr_ctx *ctx, const plsqr_sparse *a, const std::vector<int64_t> &ptr,
@@ -696,6 +717,11 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     b = ctx->b_k.data();
   }
   int rc;
+  if ((rc = magnitude_ok(b, ctx->m_k))) {
+    ctx_set_error(ctx, "b_k holds NaN, Inf or magnitudes outside [2^-500, 2^500]; scale it by a "
+                       "power of two");
+    return rc;
+  }
   CK(cudaSetDevice(ctx->opts.device));
   const int itn = args->lsqr_iteration;
   if (ctx->hist_cap < itn + 1) {

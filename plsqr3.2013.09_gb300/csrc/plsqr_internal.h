@@ -75,6 +75,10 @@ struct plsqr_ctx {
   double *d_val0 = nullptr, *dc_val0 = nullptr;  // damping values before weighting
 };
 
+// plsqr_gpu.cu: PLSQR_ERR_NUMERIC for NaN, Inf, or a largest magnitude
+// above 2^500 or (nonzero, unless allow_small) below 2^-500
+int magnitude_ok(const double *p, int64_t n, int allow_small = 0);
+
 // slab.cu
 template <typename T>
 // tgroup > 1: transpose each segment's chunks for products that stream it

@@ -100,6 +100,26 @@ def test_create_rejects_bad_matrices_before_device(pkg, bad):
     assert rc == -3 and not h.value
 
 
+@pytest.mark.parametrize("bad", ["huge", "nan"])
+def test_create_rejects_values_outside_the_norm_range(pkg, bad):
+    """Matrix values the FP64 sums of squares cannot hold (largest magnitude
+    above 2^500) or NaN: PLSQR_ERR_NUMERIC, before any device work."""
+    N = pkg._native
+    prob = pkg.generate("tiny")
+    K = prob.k_csc
+    kv = K.val.copy()
+    if bad == "huge":
+        kv[7] = 2.0 ** 520
+    else:
+        kv[7] = np.nan
+    k = _sp(N, prob.m_k, prob.n, K.ptr, K.idx, kv)
+    d, dc = prob.d_csr.as_native(), prob.d_csc.as_native()
+    h = N.vp()
+    rc = N.lib().plsqr_ctx_create(C.byref(k), C.byref(d), C.byref(dc), None, C.byref(h))
+    assert rc == -10 and not h.value
+    assert "2^500" in N.lib().plsqr_strerror(-10).decode()
+
+
 def test_create_without_device_reports_nodev(pkg, has_gpu):
     if has_gpu:
         pytest.skip("a device is visible")

@@ -298,3 +298,20 @@ def test_cli_warm_start_from_a_solution_file(pkg, problems, tmp_path):
     assert np.isfinite(r1) and r1 <= r0 * (1 + 1e-9)
     p = subprocess.run(base + ["-x0", str(x0)], cwd=tmp_path, capture_output=True, text=True)
     assert p.returncode != 0 and "mixed-precision" in p.stderr
+
+
+def test_rhs_magnitudes_scale_and_out_of_range_is_refused(pkg, problems):
+    """Scaling b by 2^480 or 2^-480 scales x by the same power of two (the
+    sums of squares of the norms still hold the values); beyond 2^500, or
+    with every entry below 2^-500, the solve is refused with
+    PLSQR_ERR_NUMERIC instead of running on an overflowed norm."""
+    prob = problems("tiny")
+    with pkg.Context(prob) as ctx:
+        ref = ctx.lsqr(lsqr_iteration=15)["x"]
+        for f in (2.0 ** 480, 2.0 ** -480):
+            x = ctx.lsqr(prob.b_k * f, lsqr_iteration=15)["x"]
+            assert rel(x / f, ref) <= 1e-13
+        for f in (2.0 ** 520, 2.0 ** -560):
+            with pytest.raises(pkg._native.PlsqrError) as e:
+                ctx.lsqr(prob.b_k * f, lsqr_iteration=15)
+            assert e.value.code == -10
