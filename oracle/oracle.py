@@ -2,8 +2,8 @@
 
 ctypes binding of lib/liboracle_plsqr.so, the C restatement of the reference
 PLSQR3 CPU path (plsqr_oracle.c).  Only tests/, __graft_entry__.smoke() and
-bench.py's CPU baseline use it, and only as the checker or the timed CPU
-baseline.  The library is built by `make -C oracle` (see build()).
+bench.py's CPU baseline use it, and only as the reference that results are
+compared with or as the timed CPU baseline.  The library is built by `make -C oracle` (see build()).
 """
 from __future__ import annotations
 

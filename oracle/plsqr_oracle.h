@@ -10,7 +10,8 @@
  * same bits as the reference built with SDVERSION=2.
  *
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this
- * library, and only as the checker or as the timed CPU baseline.
+ * library, and only as the reference that results are compared with or as
+ * the timed CPU baseline.
  */
 #ifndef PLSQR_ORACLE_H
 #define PLSQR_ORACLE_H
