@@ -2,8 +2,9 @@
 ~45 GB on the device), where the oracle would take minutes per iteration:
 size-independent properties instead of a comparison with the reference.
 The adjoint identity and linearity of the products, residual norms that
-never grow over the LSQR iterations, and the mixed-precision start-up and
-first iterations within FP32 accuracy of the FP64 ones."""
+never grow over the LSQR iterations, the mixed-precision start-up and first
+iterations within FP32 accuracy of the FP64 ones, and exact power-of-two
+scaling across a batch of right-hand sides."""
 from __future__ import annotations
 
 import numpy as np
@@ -61,3 +62,16 @@ def test_mixed_start_and_first_iterations_match_fp64(pkg, grid96):
         hm = cm.lsqr(sweeps=1, inner=5)["hist"]
     for key in ("alpha", "beta"):
         assert np.max(np.abs(hm[key] - h64[key]) / np.abs(h64[key])) <= 1e-5, key
+
+
+def test_batched_right_hand_sides_scale_exactly(pkg, grid96):
+    """k right-hand sides b, b/2 and 2b in one batch: the solutions are x,
+    x/2 and 2x bit for bit (scaling by a power of two is exact and the
+    right-hand sides do not interact)."""
+    b = grid96.b_k
+    with pkg.Context(grid96) as ctx:
+        out = ctx.batch_lsqr(np.stack([b, 0.5 * b, 2.0 * b]), sweeps=1, inner=10)
+    x = out["x"]
+    assert np.all(np.isfinite(x[0])) and np.any(x[0] != 0.0)
+    assert np.array_equal(x[1], 0.5 * x[0])
+    assert np.array_equal(x[2], 2.0 * x[0])
