@@ -65,7 +65,9 @@ struct MultiProb {
   const int64_t *dc_ptr;  // D by column
   const int32_t *dc_idx;
   const double *dc_val;
-  const int32_t *kpart;  // [nw + 1] kernel-row range of each warp of the group
+  const int32_t *korder; // [m_k] kernel rows, longest first (the lanes of a warp
+                         // then sum rows of about the same length)
+  const int32_t *kpart;  // [nw + 1] range of korder of each warp of the group
   const int32_t *cpart;  // [nw + 1] column range of each warp of the group
   const double *b;
   double *u, *v, *w, *x;
@@ -309,7 +311,8 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     // A: u = -alpha u + A v
     const double s1 = -sh.S.alpha;
     sq = 0.0;
-    for (int r = P.kpart[gw] + lane; r < P.kpart[gw + 1]; r += 32) {
+    for (int i = P.kpart[gw] + lane; i < P.kpart[gw + 1]; i += 32) {
+      const int r = P.korder[i];
       const double ur = kExact ? ld(u + r) : plsqr::dmul(ld(u + r), rb_u);
       const double y = plsqr::dadd(plsqr::dmul(s1, ur), kernel_row<kExact>(P, v, r));
       u[r] = y;
@@ -700,15 +703,25 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
     memset(&d, 0, sizeof(d));
     const int32_t m_k = q.k_csc.num_row, n = q.k_csc.num_col, m_d = q.d_csr.num_row;
     const int nw = nb[(size_t)mp->group_of[(size_t)p]] * kMW;
-    std::vector<int32_t> kp, cp;
-    split_by_nnz(kr[(size_t)p], nw, kp);
+    std::vector<int32_t> kp, cp, ko((size_t)m_k);
+    {  // kernel rows longest first; the warps' ranges balanced in that order
+      const std::vector<int64_t> &rp = kr[(size_t)p];
+      for (int32_t r = 0; r < m_k; ++r) ko[(size_t)r] = r;
+      std::stable_sort(ko.begin(), ko.end(), [&](int32_t a, int32_t b) {
+        return rp[(size_t)a + 1] - rp[(size_t)a] > rp[(size_t)b + 1] - rp[(size_t)b];
+      });
+      std::vector<int64_t> pre((size_t)m_k + 1, 0);
+      for (int32_t i = 0; i < m_k; ++i)
+        pre[(size_t)i + 1] = pre[(size_t)i] + (rp[(size_t)ko[(size_t)i] + 1] - rp[(size_t)ko[(size_t)i]]);
+      split_by_nnz(pre, nw, kp);
+    }
     std::vector<int64_t> pre((size_t)n + 1);
     for (int32_t c = 0; c <= n; ++c)
       pre[(size_t)c] = kc[(size_t)p][(size_t)c] + dc[(size_t)p][(size_t)c];
     split_by_nnz(pre, nw, cp);
     const int64_t m = (int64_t)m_k + m_d;
     int64_t *kr_ptr, *kc_ptr, *dr_ptr, *dc_ptr;
-    int32_t *kr_idx, *kc_idx, *dr_idx, *dc_idx, *kpart, *cpart;
+    int32_t *kr_idx, *kc_idx, *dr_idx, *dc_idx, *kpart, *cpart, *korder;
     double *kr_val, *kc_val, *dr_val, *dc_val, *b, *u, *v, *w, *x;
     if ((rc = upload(mp, &kr_ptr, kr[(size_t)p].data(), kr[(size_t)p].size())) ||
         (rc = upload(mp, &kr_idx, kri[(size_t)p].data(), kri[(size_t)p].size())) ||
@@ -722,6 +735,7 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
         (rc = upload(mp, &dc_ptr, dc[(size_t)p].data(), dc[(size_t)p].size())) ||
         (rc = upload(mp, &dc_idx, q.d_csc.idx, (size_t)q.d_csc.nnz)) ||
         (rc = upload(mp, &dc_val, q.d_csc.val, (size_t)q.d_csc.nnz)) ||
+        (rc = upload(mp, &korder, ko.data(), ko.size())) ||
         (rc = upload(mp, &kpart, kp.data(), kp.size())) ||
         (rc = upload(mp, &cpart, cp.data(), cp.size())) ||
         (rc = upload(mp, &b, q.b_k, (size_t)m_k)) ||
@@ -734,7 +748,7 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
     d.kc_ptr = kc_ptr, d.kc_idx = kc_idx, d.kc_val = kc_val;
     d.dr_ptr = dr_ptr, d.dr_idx = dr_idx, d.dr_val = dr_val;
     d.dc_ptr = dc_ptr, d.dc_idx = dc_idx, d.dc_val = dc_val;
-    d.kpart = kpart, d.cpart = cpart;
+    d.korder = korder, d.kpart = kpart, d.cpart = cpart;
     d.b = b, d.u = u, d.v = v, d.w = w, d.x = x;
     d.m_k = m_k, d.m_d = m_d, d.n = n, d.iters = q.lsqr_iteration, d.itnlim = q.itnlim;
     d.damp = q.damp, d.atol = q.atol, d.btol = q.btol;
