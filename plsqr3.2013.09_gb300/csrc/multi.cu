@@ -409,7 +409,7 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
 
 // The persistent kernel: block b runs the queue of its group.
 template <bool kExact>
-__global__ void __launch_bounds__(kMT)
+__global__ void __launch_bounds__(kMT, 4)  // 4 blocks per SM (64 registers)
     k_multi_lsqr(const MultiProb *__restrict__ probs, const MultiGroup *__restrict__ groups,
                  const int32_t *__restrict__ queue, const int32_t *__restrict__ block_group,
                  unsigned int *bars, double *parts, DevState *out, int *err, long long wait_ns) {

@@ -62,8 +62,10 @@ def test_matches_oracle(pkg, orc, uneven, exact):
 
 def test_queues_when_problems_outnumber_blocks(pkg):
     base = pkg.CONFIGS["tiny"]
+    with pkg.multi.Multi([pkg.generate("tiny")], iterations=1) as probe:
+        count = probe.info()["blocks"] + 64  # the launch's block count plus a queue
     probs = [pkg.generate(dict(base, seed=1000 + i, n_rays=20 + (i % 7) * 10))
-             for i in range(520)]
+             for i in range(count)]
     with pkg.multi.Multi(probs, iterations=12) as mp:
         info = mp.info()
         assert info["count"] > info["blocks"]
