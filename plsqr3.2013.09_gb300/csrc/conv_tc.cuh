@@ -1,27 +1,19 @@
-// 3x3x3 convolution of a channels-last BF16 block as an implicit GEMM on the
-// fifth-generation tensor cores: tcgen05.mma (kind::f16, BF16 operands, FP32
-// accumulator in tensor memory), no im2col matrix in HBM.
+// The warm-start network's contractions on the fifth-generation tensor
+// cores: tcgen05.mma (kind::f16, BF16 operands, FP32 accumulator in tensor
+// memory), one elected thread issuing the MMAs, tcgen05.ld epilogues (warp w
+// reads TMEM lanes 32w..32w+31).
 //
-// One CTA owns 128 consecutive voxels (the MMA's M).  For each of the 27
-// taps t it gathers the neighbours' channel rows A_t[r][k] = X[p0 + r +
-// offset(t)][k] (zero outside the grid) and the weight block B_t[o][k] into
-// shared memory with cp.async, and one elected thread issues CI/16 MMAs of
-// 128 x CO x 16 that accumulate into the CTA's TMEM columns.  Three stages
-// keep the gathers of later taps in flight while the tensor core works; a
-// stage is refilled only after the MMAs that read it have committed to its
-// mbarrier.  The epilogue reads the accumulator back with tcgen05.ld (warp w
-// owns TMEM lanes 32w..32w+31, i.e. voxels p0 + 32w + lane).
-//
-// The same kernel computes the input gradient of a convolution: the
-// gathered block is dz (CO_layer channels), the taps are mirrored
-// (offset(26 - t) = -offset(t)) and B_t[ci][co] is read from the transposed
-// weights, so dX[p][ci] = sum_t sum_co dz[p - offset(t)][co] W[co][t][ci].
+// k_conv_tc2: a 3x3x3 convolution of a channels-last BF16 block as an
+// implicit GEMM (no im2col matrix in HBM); its input gradient is the same
+// kernel on dz with mirrored taps (offset(26 - t) = -offset(t)) and
+// B_t[ci][co] read from the transposed weights, so dX[p][ci] = sum_t sum_co
+// dz[p - offset(t)][co] W[co][t][ci].  k_gemm_tc: the weight gradient's
+// split-K GEMM.
 //
 // Shared-memory operands use the canonical K-major layout without swizzle:
-// 8-row x 16-byte core matrices, core (g, j) of a tile at byte
-// (g * CI/8 + j) * 128, so the descriptor's leading byte offset (between
-// core matrices along K) is 128 and its stride byte offset (between 8-row
-// groups) is CI/8 * 128.
+// 8-row x 16-byte core matrices; the descriptor's leading byte offset is the
+// step between core matrices along K and its stride byte offset the step
+// between 8-row groups.
 //
 // Every wait on an mbarrier is bounded (one second of the global timer); a
 // wait that runs out sets *err, skips the remaining MMAs and the epilogue,
@@ -38,11 +30,10 @@ namespace nn {
 
 constexpr int kTcRows = 128;    // voxels per CTA (MMA M)
 constexpr int kTcThreads = 128; // four warps
-constexpr int kTcStages = 3;
 constexpr unsigned long long kTcWaitNs = 1000000000ull;
 
 struct ConvTcArgs {
-  const __nv_bfloat16 *x;  // gathered block [n][CI]
+  const __nv_bfloat16 *x;  // input block [n][CI]
   const __nv_bfloat16 *w;  // B_t[o][k] = w[tap(t) * tap_stride + o * ldw + k]
   int64_t ldw, tap_stride;
   int flip;                // tap(t) = flip ? 26 - t : t; neighbour offset(t) either way
@@ -128,184 +119,6 @@ __host__ __device__ constexpr uint32_t tc_cols(int co) {
   return co <= 32 ? 32u : co <= 64 ? 64u : co <= 128 ? 128u : 256u;
 }
 
-template <int CI, int CO>
-struct ConvTcShape {
-  static_assert(CI % 16 == 0 && CO % 16 == 0 && CO >= 16 && CO <= 256, "channel counts");
-  static constexpr int kCoresK = CI / 8;
-  static constexpr int kABytes = kTcRows * CI * 2;
-  static constexpr int kBBytes = CO * CI * 2;
-  static constexpr int kStageBytes = kABytes + kBBytes;
-  // stages, then the stage mbarriers and the TMEM address slot; +128 for
-  // aligning the dynamic block
-  static constexpr int kSmemBytes = kTcStages * kStageBytes + 64 + 128;
-};
-
-template <int CI, int CO>
-__global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvTcArgs a) {
-  using S = ConvTcShape<CI, CO>;
-  extern __shared__ uint8_t tc_smem_raw[];
-  uint8_t *smem = reinterpret_cast<uint8_t *>(
-      (reinterpret_cast<uintptr_t>(tc_smem_raw) + 127) & ~(uintptr_t)127);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcStages * S::kStageBytes);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + kTcStages);
-  __shared__ int abort_flag;
-
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t n = a.g.n();
-  const int64_t p0 = (int64_t)blockIdx.x * kTcRows;
-  constexpr uint32_t kCols = tc_cols(CO);
-  constexpr uint32_t kIdesc = tc_idesc(kTcRows, CO);
-  constexpr uint32_t kSbo = S::kCoresK * 128;
-
-  if (tid == 0) {
-    abort_flag = 0;
-    for (int s = 0; s < kTcStages; ++s)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(tslot)),
-                 "r"(kCols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tslot;
-
-  // this thread's gather rows: task q = it * 128 + tid, row q / (CI/8),
-  // chunk q % (CI/8); the voxel coordinates of each row, computed once
-  constexpr int kTasksA = kTcRows * S::kCoresK / kTcThreads;  // = CI/8
-  int vx[kTasksA], vy[kTasksA], vz[kTasksA];
-#pragma unroll
-  for (int it = 0; it < kTasksA; ++it) {
-    const int q = it * kTcThreads + tid;
-    const int64_t p = p0 + q / S::kCoresK;
-    if (p < n) {
-      vx[it] = (int)(p % a.g.nx);
-      vy[it] = (int)((p / a.g.nx) % a.g.ny);
-      vz[it] = (int)(p / ((int64_t)a.g.nx * a.g.ny));
-    } else {
-      vx[it] = -4;  // outside for every tap
-      vy[it] = 0;
-      vz[it] = 0;
-    }
-  }
-
-  auto gather = [&](int t, int s) {
-    uint8_t *A = smem + s * S::kStageBytes;
-    uint8_t *B = A + S::kABytes;
-    const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-#pragma unroll
-    for (int it = 0; it < kTasksA; ++it) {
-      const int q = it * kTcThreads + tid;
-      const int r = q / S::kCoresK, j = q % S::kCoresK;
-      const int xx = vx[it] + dx, yy = vy[it] + dy, zz = vz[it] + dz;
-      const bool in = xx >= 0 && xx < a.g.nx && yy >= 0 && yy < a.g.ny && zz >= 0 && zz < a.g.nz;
-      const __nv_bfloat16 *src =
-          in ? a.x + (((int64_t)zz * a.g.ny + yy) * a.g.nx + xx) * CI + j * 8 : a.x;
-      const uint32_t dst = smem_u32(A + ((r >> 3) * S::kCoresK + j) * 128 + (r & 7) * 16);
-      cp_async16(dst, src, in ? 16u : 0u);
-    }
-    const int tap = a.flip ? 26 - t : t;
-    const __nv_bfloat16 *wt = a.w + (int64_t)tap * a.tap_stride;
-    for (int q = tid; q < CO * S::kCoresK; q += kTcThreads) {
-      const int o = q / S::kCoresK, j = q % S::kCoresK;
-      const uint32_t dst = smem_u32(B + ((o >> 3) * S::kCoresK + j) * 128 + (o & 7) * 16);
-      cp_async16(dst, wt + (int64_t)o * a.ldw + j * 8, 16u);
-    }
-  };
-
-  bool ok = true;  // this thread's waits all completed
-  auto wait_mma = [&](int t) {  // the MMAs of tap t have read their stage
-    if (!ok) return;
-    if (!mbar_wait(smem_u32(&bars[t % kTcStages]), (uint32_t)((t / kTcStages) & 1))) {
-      ok = false;
-      abort_flag = 1;
-      atomicExch(a.err, 1u);
-    }
-  };
-
-#pragma unroll 1
-  for (int t = 0; t < kTcStages - 1; ++t) {
-    gather(t, t);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-  }
-#pragma unroll 1
-  for (int t = 0; t < 27; ++t) {
-    const int tn = t + kTcStages - 1;
-    if (tn < 27) {
-      if (t >= 1) wait_mma(t - 1);  // stage tn % S last held tap t - 1
-      gather(tn, tn % kTcStages);
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    asm volatile("cp.async.wait_group %0;" ::"n"(kTcStages - 1) : "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0 && !abort_flag) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int s = t % kTcStages;
-      const uint32_t A = smem_u32(smem + s * S::kStageBytes);
-      const uint32_t B = A + S::kABytes;
-#pragma unroll
-      for (int kk = 0; kk < CI / 16; ++kk)
-        tc_mma(tmem, tc_desc(A + kk * 256, 128, kSbo), tc_desc(B + kk * 256, 128, kSbo), kIdesc,
-               (t > 0 || kk > 0) ? 1u : 0u);
-      tc_commit(smem_u32(&bars[s]));
-    }
-  }
-  // the last commit follows every MMA of the CTA
-  wait_mma(26);
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
-  if (!abort_flag) {
-    const int64_t p = p0 + warp * 32 + lane;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll
-    for (int c0 = 0; c0 < CO; c0 += 16) {
-      uint32_t v[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-            "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-          : "r"(trow + (uint32_t)c0));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      float f[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        f[i] = __uint_as_float(v[i]);
-        if (a.bias) f[i] += a.bias[c0 + i];
-        if (a.relu) f[i] = fmaxf(f[i], 0.f);
-      }
-      if (p < n) {
-        if (a.out_bf16) {
-          __align__(16) __nv_bfloat16 h[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) h[i] = __float2bfloat16(f[i]);
-          uint4 *d = reinterpret_cast<uint4 *>(a.out_bf16 + p * CO + c0);
-          d[0] = reinterpret_cast<const uint4 *>(h)[0];
-          d[1] = reinterpret_cast<const uint4 *>(h)[1];
-        } else {
-          float4 *d = reinterpret_cast<float4 *>(a.out_f32 + p * CO + c0);
-#pragma unroll
-          for (int i = 0; i < 4; ++i) d[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
-        }
-      }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols)
-                 : "memory");
-}
-
 // The same convolution with the input block staged once: a CTA owns an
 // 8 (x) x 16 (y) x 1 (z) brick of voxels (the MMA's 128 rows: row r is voxel
 // (x0 + r % 8, y0 + r / 8, z)) and loads the brick's halo, 10 x 18 x 3
@@ -319,7 +132,10 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc(ConvTcArgs a) {
 // halo is read 540 / 128 = 4.2 times per output voxel instead of 27.  The
 // loads are committed per plane, so that the MMAs of plane dz = -1 run while
 // the other two planes arrive.
-template <int CI, int CO>
+// kAllW: all 27 weight taps stay in shared memory; otherwise (layers whose
+// halo and 27 taps exceed 227 KB) one plane's 9 taps at a time, each plane's
+// taps loaded once the MMAs of the previous plane have read theirs.
+template <int CI, int CO, bool kAllW>
 struct ConvTc2Shape {
   static_assert(CI % 16 == 0 && CO % 16 == 0 && CO >= 16 && CO <= 256, "channel counts");
   static constexpr int kCoresK = CI / 8;
@@ -327,19 +143,21 @@ struct ConvTc2Shape {
   static constexpr int kPlaneBytes = 18 * kLineBytes;
   static constexpr int kHaloBytes = 3 * kPlaneBytes;
   static constexpr int kTapBytes = CO * CI * 2;          // one tap's B tile
-  static constexpr int kSmemBytes = kHaloBytes + 27 * kTapBytes + 64 + 128;
+  static constexpr int kWTaps = kAllW ? 27 : 9;
+  static constexpr int kSmemBytes = kHaloBytes + kWTaps * kTapBytes + 64 + 128;
 };
 
-template <int CI, int CO>
+template <int CI, int CO, bool kAllW>
 __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
-  using S = ConvTc2Shape<CI, CO>;
+  using S = ConvTc2Shape<CI, CO, kAllW>;
   extern __shared__ uint8_t tc_smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(tc_smem_raw) + 127) & ~(uintptr_t)127);
   uint8_t *halo = smem;
   uint8_t *wts = smem + S::kHaloBytes;
-  uint64_t *bar = reinterpret_cast<uint64_t *>(wts + 27 * S::kTapBytes);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(wts + S::kWTaps * S::kTapBytes);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+  __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int bxn = (a.g.nx + 7) / 8, byn = (a.g.ny + 15) / 16;
@@ -350,6 +168,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
   constexpr uint32_t kIdesc = tc_idesc(kTcRows, CO);
 
   if (tid == 0) {
+    abort_flag = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -361,7 +180,20 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
 
-  // loads, one cp.async group per plane: its 180 halo voxels and its 9 taps
+  // plane s's 9 weight taps into their slots (all 27 slots, or 9 reused)
+  auto load_taps = [&](int s) {
+    for (int q = tid; q < 9 * CO * S::kCoresK; q += kTcThreads) {
+      const int j = q % S::kCoresK, o = (q / S::kCoresK) % CO, t = s * 9 + q / (S::kCoresK * CO);
+      const int tap = a.flip ? 26 - t : t;
+      const __nv_bfloat16 *src = a.w + (int64_t)tap * a.tap_stride + (int64_t)o * a.ldw + j * 8;
+      cp_async16(smem_u32(wts + (t % S::kWTaps) * S::kTapBytes + ((o >> 3) * S::kCoresK + j) * 128 +
+                          (o & 7) * 16),
+                 src, 16u);
+    }
+  };
+
+  // loads, one cp.async group per plane: its 180 halo voxels and (all
+  // weights resident, or plane 0) its 9 taps
 #pragma unroll 1
   for (int s = 0; s < 3; ++s) {
     const int zz = z + s - 1;
@@ -375,13 +207,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
       cp_async16(smem_u32(halo + s * S::kPlaneBytes + (l * S::kCoresK + j) * 160 + v * 16), src,
                  in ? 16u : 0u);
     }
-    for (int q = tid; q < 9 * CO * S::kCoresK; q += kTcThreads) {
-      const int j = q % S::kCoresK, o = (q / S::kCoresK) % CO, t = s * 9 + q / (S::kCoresK * CO);
-      const int tap = a.flip ? 26 - t : t;
-      const __nv_bfloat16 *src = a.w + (int64_t)tap * a.tap_stride + (int64_t)o * a.ldw + j * 8;
-      cp_async16(smem_u32(wts + t * S::kTapBytes + ((o >> 3) * S::kCoresK + j) * 128 + (o & 7) * 16),
-                 src, 16u);
-    }
+    if (kAllW || s == 0) load_taps(s);
     asm volatile("cp.async.commit_group;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -389,30 +215,48 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
 
+  bool ok = true;
 #pragma unroll 1
   for (int s = 0; s < 3; ++s) {
-    if (s == 0) asm volatile("cp.async.wait_group 2;" ::: "memory");
-    else if (s == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
-    else asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (kAllW) {
+      if (s == 0) asm volatile("cp.async.wait_group 2;" ::: "memory");
+      else if (s == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
+      else asm volatile("cp.async.wait_group 0;" ::: "memory");
+    } else {
+      if (s > 0) {
+        // plane s - 1's MMAs (the commit's phase s - 1) have read the slots
+        if (ok && !mbar_wait(smem_u32(bar), (uint32_t)((s - 1) & 1))) {
+          ok = false;
+          abort_flag = 1;
+          atomicExch(a.err, 1u);
+        }
+        load_taps(s);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 2;" ::: "memory");
+      }
+      if (s > 0) asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (tid == 0) {
+    if (tid == 0 && !abort_flag) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t hp = smem_u32(halo + s * S::kPlaneBytes);
 #pragma unroll 1
       for (int tt = 0; tt < 9; ++tt) {
         const int t = s * 9 + tt, dy = tt / 3, dx = tt % 3;  // dy + 1, dx + 1
         const uint32_t A = hp + dy * S::kLineBytes + dx * 16;
-        const uint32_t B = smem_u32(wts + t * S::kTapBytes);
+        const uint32_t B = smem_u32(wts + (t % S::kWTaps) * S::kTapBytes);
 #pragma unroll
         for (int kk = 0; kk < CI / 16; ++kk)
           tc_mma(tmem, tc_desc(A + kk * 320, 160, S::kLineBytes),
                  tc_desc(B + kk * 256, 128, S::kCoresK * 128), kIdesc, (t > 0 || kk > 0) ? 1u : 0u);
       }
-      if (s == 2) tc_commit(smem_u32(bar));
+      if (!kAllW || s == 2) tc_commit(smem_u32(bar));  // phase s (streamed) or 0
     }
   }
-  const bool ok = mbar_wait(smem_u32(bar), 0u);
+  // the last commit follows every MMA: phase 2 (streamed taps) or 0
+  if (ok && !abort_flag && !mbar_wait(smem_u32(bar), 0u)) ok = false;
   if (!ok) atomicExch(a.err, 1u);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int r = warp * 32 + lane;
@@ -469,7 +313,8 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
 // rows of A and one voxel range (split); stages of 64 voxels are loaded by
 // cp.async into the canonical K-major layout (core (g, j) at (g * 8 + j) *
 // 128 bytes: leading byte offset 128, stride byte offset 1024) and consumed
-// by 4 MMAs each, with the same mbarrier pipeline as k_conv_tc.  The splits
+// by 4 MMAs each; a stage is refilled once the MMAs that read it have
+// committed to its mbarrier.  The splits
 // are added in split order by k_gemm_tc_reduce.
 struct GemmTcArgs {
   const __nv_bfloat16 *A;  // [M][K]

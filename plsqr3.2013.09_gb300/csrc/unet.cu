@@ -141,31 +141,31 @@ int init_conv(plsqr_unet *net, Conv &L, int cin, int cout, Grid3 g, int fan_c, u
   return PLSQR_OK;
 }
 
-// The halo-staged kernel where its halo and all 27 weight taps fit in one
-// CTA's shared memory, else the kernel that gathers tap by tap.
-template <int CI, int CO>
-int conv_tc_run(plsqr_unet *net, const ConvTcArgs &a) {
+// The halo-staged kernel, with all 27 weight taps resident where they fit
+// in one CTA's shared memory beside the halo, else one plane's taps at a time.
+template <int CI, int CO, bool kAllW>
+int conv_tc_launch(plsqr_unet *net, const ConvTcArgs &a) {
   // at most 512 / cols CTAs per SM (of 228 KB of shared memory), so that
   // every resident CTA's tensor-memory allocation succeeds at once
   constexpr uint32_t cols = tc_cols(CO);
   constexpr int floor_bytes = cols >= 128 ? 58 * 1024 : cols >= 64 ? 30 * 1024 : 0;
-  constexpr int kMax = 227 * 1024;
-  if constexpr (ConvTc2Shape<CI, CO>::kSmemBytes <= kMax) {
-    constexpr int need = ConvTc2Shape<CI, CO>::kSmemBytes;
-    constexpr int bytes = need > floor_bytes ? need : floor_bytes;
-    UK(cudaFuncSetAttribute(k_conv_tc2<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    const int64_t blocks = (int64_t)((a.g.nx + 7) / 8) * ((a.g.ny + 15) / 16) * a.g.nz;
-    k_conv_tc2<CI, CO><<<(unsigned)blocks, kTcThreads, bytes, net->stream>>>(a);
-  } else {
-    constexpr int need = ConvTcShape<CI, CO>::kSmemBytes;
-    constexpr int bytes = need > floor_bytes ? need : floor_bytes;
-    static_assert(bytes <= kMax, "shared memory of one CTA");
-    UK(cudaFuncSetAttribute(k_conv_tc<CI, CO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    const int64_t blocks = (a.g.n() + kTcRows - 1) / kTcRows;
-    k_conv_tc<CI, CO><<<(unsigned)blocks, kTcThreads, bytes, net->stream>>>(a);
-  }
+  constexpr int need = ConvTc2Shape<CI, CO, kAllW>::kSmemBytes;
+  constexpr int bytes = need > floor_bytes ? need : floor_bytes;
+  static_assert(bytes <= 227 * 1024, "shared memory of one CTA");
+  UK(cudaFuncSetAttribute(k_conv_tc2<CI, CO, kAllW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          bytes));
+  const int64_t blocks = (int64_t)((a.g.nx + 7) / 8) * ((a.g.ny + 15) / 16) * a.g.nz;
+  k_conv_tc2<CI, CO, kAllW><<<(unsigned)blocks, kTcThreads, bytes, net->stream>>>(a);
   UK(cudaGetLastError());
   return PLSQR_OK;
+}
+
+template <int CI, int CO>
+int conv_tc_run(plsqr_unet *net, const ConvTcArgs &a) {
+  if constexpr (ConvTc2Shape<CI, CO, true>::kSmemBytes <= 227 * 1024)
+    return conv_tc_launch<CI, CO, true>(net, a);
+  else
+    return conv_tc_launch<CI, CO, false>(net, a);
 }
 
 // The channel pairs of the network's layers (forward: cin -> cout; input
