@@ -96,6 +96,10 @@ def torch_ops():
         return _OPS
     import torch
 
+    if hasattr(torch.ops.plsqr, "unet_predict"):  # registered by another copy of this module
+        _OPS = torch.ops.plsqr
+        return _OPS
+
     def _vol(t, name: str):
         if t.dtype != torch.float32 or not t.is_cuda:
             raise ValueError(f"{name} must be a float32 CUDA tensor")
