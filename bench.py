@@ -134,15 +134,43 @@ def dist():
     return ws, rank, local
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(pkg, orc, prob, iterations: int) -> dict:
-    """The oracle port (FP64, OpenMP on every host thread) timed on a few
-    LSQR iterations of the same problem; GB/s of the same algorithmic bytes."""
+    """The oracle port (FP64, OpenMP on every host thread) on `iterations`
+    LSQR iterations of the same problem, timed over the iteration loop only:
+    the region of the reference's own "Parallel LSQR time" (source/lsqr.c:
+    476-478, 836-842), start-up excluded."""
     o = orc.OracleProblem(prob)
     threads = orc.get_threads()
     t0 = time.perf_counter()
-    o.lsqr(iterations)
-    dt = time.perf_counter() - t0
-    return dict(seconds=dt, iterations=iterations, threads=threads)
+    r = o.lsqr(iterations)
+    wall = time.perf_counter() - t0
+    return dict(seconds=r["result"]["loop_seconds"], wall_seconds=wall, iterations=iterations,
+                threads=threads)
+
+
+def cpu_sample_text(cfg: str, iterations: int, steps: int = 1) -> str:
+    return (f"{steps} x {iterations} LSQR iterations of the {cfg} solve, timed over the "
+            f"iteration loop only (the reference's 'Parallel LSQR time' region, start-up "
+            f"excluded); host CPU {cpu_model()}")
 
 
 def max_over_ranks(values: list[float]) -> list[float]:
@@ -173,7 +201,8 @@ def main() -> int:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="grid96")
     ap.add_argument("--iterations", type=int, default=None)
-    ap.add_argument("--cpu-iterations", type=int, default=2)
+    ap.add_argument("--cpu-iterations", type=int, default=5,
+                    help="LSQR iterations of each CPU baseline sample (loop timed alone)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tts", action="store_true", help="skip the time-to-1e-6 runs")
     ap.add_argument("--profile", action="store_true",
@@ -215,7 +244,7 @@ def main() -> int:
         prob = pkg.generate(args.config)
         bytes_it = algorithmic_bytes(prob)
         per = []
-        for _ in range(args.warmup if args.warmup < 1 else 1):
+        for _ in range(min(args.warmup, 1)):
             cpu_sample(pkg, orc, prob, 1)
         for _ in range(args.steps):
             s = cpu_sample(pkg, orc, prob, args.cpu_iterations)
@@ -230,9 +259,10 @@ def main() -> int:
                 "data": "synthetic (seeded generator, reference file formats)",
                 "config": workload(args.config, prob, iters),
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": per[0]["threads"],
-                                 "kind": "port",
-                                 "sample": f"{args.cpu_iterations} LSQR iterations (plus start-up) "
-                                           f"per step of the {args.config} solve"},
+                                 "kind": "port", "cpu_model": cpu_model(),
+                                 "seconds_per_iteration": secs / its,
+                                 "sample": cpu_sample_text(args.config, args.cpu_iterations,
+                                                           args.steps)},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -335,9 +365,10 @@ def main() -> int:
         orc = graft.load_oracle()
         s = cpu_sample(pkg, orc, prob, args.cpu_iterations)
         cpu = {"value": bytes_it * s["iterations"] / s["seconds"] / 1e9, "unit": UNIT,
-               "cores": s["threads"], "kind": "port",
-               "sample": f"{s['iterations']} LSQR iterations (plus start-up) of the same solve, "
-                         f"{s['seconds']:.1f} s"}
+               "cores": s["threads"], "kind": "port", "cpu_model": cpu_model(),
+               "seconds_per_iteration": s["seconds"] / s["iterations"],
+               "sample": cpu_sample_text(args.config, s["iterations"])
+                         + f", {s['seconds']:.1f} s"}
     if rank != 0:
         return 0
     # per solve: start-up (sum of squares, norm, A^T y as slab product +

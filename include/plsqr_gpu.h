@@ -49,6 +49,16 @@ extern "C" {
 #define PLSQR_PREC_FP64 0  /* FP64 values, vectors, reductions              */
 #define PLSQR_PREC_MIXED 1 /* FP32 inner sweeps on the value split, FP64 outer */
 
+/* Order of the FP64 sums (PLSQR_PREC_FP64 contexts). */
+#define PLSQR_ORDER_FAST 0      /* products and norms summed in parallel order
+                                   (default; results within rounding of the
+                                   reference's, not its bits)                 */
+#define PLSQR_ORDER_REFERENCE 1 /* every product, sum and norm in the order and
+                                   rounding of the reference's CPU code
+                                   (CPUSpMV.c, mycblas.c, lsqr.c built for FP64
+                                   without FMA contraction): a solve returns the
+                                   reference's bits, at a fraction of the speed */
+
 /* Compressed sparse matrix, by column (ptr over columns, idx = row) or by
  * row (ptr over rows, idx = column); SpMatCSC / SpMatCSR of
  * source/main.h:123-130, 158-165.  Exactly one of ptr32 / ptr64 is set, so
@@ -87,7 +97,7 @@ typedef struct {
    * product visits the columns in 3-D Morton order so that cells sharing
    * rays are gathered together.  Zeros: natural column order. */
   int32_t grid[3];
-  int32_t pad;
+  int32_t order; /* PLSQR_ORDER_* (FP64 contexts; mixed precision needs FAST) */
 } plsqr_opts;
 
 typedef struct {
@@ -218,11 +228,28 @@ int plsqr_bench_aprod(plsqr_ctx *ctx, int mode, int reps, double *ms_per_launch)
  * preceding plsqr_lsqr on the context (state and history are overwritten). */
 int plsqr_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration);
 
+/* ---- timing report: the reference's GPTL timers (source/lsqr.c:473-842,
+ *      aprod_impl.c:69-497; gptl.c writes them to timing.<rank>) ----------- */
+/* on = 1: the following FP64 solves on the context run their iterations
+ * without the CUDA graph and record CUDA events around five regions of every
+ * iteration, named after the reference's timers: spmv, norm1, spmvT,
+ * update_x, krylov_p1 (each region's "covers" text in the report lists the
+ * reference timers whose work it holds); the host side of every region is
+ * an NVTX range of the same name.  Without timing, the solve is one NVTX
+ * range "LSQR_MAIN_ITERATION" around graph launches.  on = 0 restores the
+ * graph replay. */
+int plsqr_set_timing(plsqr_ctx *ctx, int on);
+/* JSON report of the last timed solve: LSQR_MAIN_ITERATION seconds, the
+ * start-up, per region the total, mean, min and max, and every iteration's
+ * time per region.  PLSQR_ERR_STATE when no timed solve has run. */
+int plsqr_write_timing(const plsqr_ctx *ctx, const char *path);
+
 /* ---- product without device allocation ----------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
- * memory: code running inside CUDA stream capture (cudaMalloc is not allowed
- * there), code whose device memory belongs to another allocator or a fixed
- * budget, and callers that cannot block on the driver's allocator.
+ * memory: code whose device memory belongs to another allocator or a fixed
+ * budget (a framework's caching allocator, an MPI rank that sized its
+ * buffers before the solve), and callers that cannot block on the driver's
+ * allocator (cudaMalloc and cudaFree may synchronise the device).
  * y <- y + A x for an n_rows-row CSR matrix (row_ptr int64[n_rows+1],
  * col_idx/val 16-byte aligned, indices in range of x) and *nrm2 = ||y||_2
  * after the update; every pointer is device memory, the work is ordered on
@@ -231,8 +258,10 @@ int plsqr_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration);
  * 128 KB static device array of the library (held by every GPU that loads the
  * library until exit), so n_rows is limited to PLSQR_NOALLOC_MAX_ROWS
  * (PLSQR_ERR_ARG beyond it).  The first call on a device looks up that array
- * and should come before any stream capture; calls share the array, so calls
- * that overlap on the GPU race. */
+ * and should come before any stream capture (a first call on a capturing
+ * stream returns PLSQR_ERR_STATE and does nothing); calls share the array,
+ * so calls that overlap on the GPU race.  The looked-up address is kept for
+ * the process: calls after a cudaDeviceReset are not supported. */
 #define PLSQR_NOALLOC_MAX_ROWS 1048576
 int plsqr_aprod1_nrm2_noalloc(int32_t n_rows, const int64_t *row_ptr,
                               const int32_t *col_idx, const double *val,
@@ -444,7 +473,15 @@ typedef struct {
   int32_t pad;
   double noise_frac;        /* noise sigma / rms(K x_true)                   */
   double damp_identity;     /* identity damping weight                       */
-  double damp_lap;          /* second-difference damping weight              */
+  double damp_lap;          /* second-difference damping weight (xx, yy, zz) */
+  double damp_cross;        /* cross-difference weight (xy, xz, yz rows of
+                               damping_binary.py:291-511); 0 leaves those rows
+                               out                                           */
+  int32_t n_params;         /* parameter fields of the model (damping_binary.py
+                               np): the damping matrix repeats per field, with
+                               columns offset by nx*ny*nz and rows by the rows
+                               of one field; 0 or 1 = one field               */
+  int32_t pad2;
   uint64_t seed;
 } plsqr_synth_params;
 

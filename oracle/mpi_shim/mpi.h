@@ -87,6 +87,8 @@ int MPI_Allreduce(const void *sbuf, void *rbuf, int count, MPI_Datatype dt,
 int MPI_Bcast(void *buf, int count, MPI_Datatype dt, int root, MPI_Comm comm);
 int MPI_Allgather(const void *sbuf, int scount, MPI_Datatype sdt, void *rbuf,
                   int rcount, MPI_Datatype rdt, MPI_Comm comm);
+int MPI_Scatter(const void *sbuf, int scount, MPI_Datatype sdt, void *rbuf,
+                int rcount, MPI_Datatype rdt, int root, MPI_Comm comm);
 int MPI_Scatterv(const void *sbuf, const int *scounts, const int *displs,
                  MPI_Datatype sdt, void *rbuf, int rcount, MPI_Datatype rdt,
                  int root, MPI_Comm comm);

@@ -8,6 +8,7 @@ compared with or as the timed CPU baseline.  The library is built by `make -C or
 from __future__ import annotations
 
 import ctypes as C
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -17,6 +18,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "lib" / "liboracle_plsqr.so"
 REF_BIN = HERE / "_ref" / "PLSQR3"
+# the reference's source directory, for the recipes that compile the
+# reference program itself (make ref / ref_gpu_aprod); overridable like the
+# Makefile's REF_SRC
+REF_SRC = Path(os.environ.get("PLSQR_REF_SRC", "/root/reference/source"))
 
 vp = C.c_void_p
 
@@ -40,17 +45,27 @@ class Result(C.Structure):
     _fields_ = [("istop", C.c_int), ("itn", C.c_int), ("anorm", C.c_double),
                 ("acond", C.c_double), ("rnorm", C.c_double), ("arnorm_out", C.c_double),
                 ("xnorm", C.c_double), ("arnorm", C.c_double), ("bnorm", C.c_double),
-                ("dxmax", C.c_double), ("maxdx", C.c_int)]
+                ("dxmax", C.c_double), ("maxdx", C.c_int), ("loop_seconds", C.c_double)]
 
 
 _lib = None
+
+# int (*)(int mode, int m, int n, oracle_problem *p, void *usr, int is_final, int iteration)
+APROD_FN = C.CFUNCTYPE(C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(Problem), vp, C.c_int,
+                       C.c_int)
 
 
 def build(with_reference: bool = False) -> None:
     """make -C oracle (and `make ref` when the reference tree is mounted)."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    if with_reference and Path("/root/reference/source/lsqr.c").exists() and shutil.which("gcc"):
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", "-j8"], check=True)
+    if with_reference and reference_available():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", "-j8", f"REF_SRC={REF_SRC}"],
+                       check=True)
+
+
+def reference_available() -> bool:
+    """The reference sources are present and a C compiler can build them."""
+    return (REF_SRC / "lsqr.c").exists() and shutil.which("gcc") is not None
 
 
 REF_GPU_APROD_BIN = HERE / "_ref" / "PLSQR3_gpu_aprod"
@@ -59,9 +74,10 @@ REF_GPU_APROD_BIN = HERE / "_ref" / "PLSQR3_gpu_aprod"
 def build_gpu_aprod():
     """The reference program linked with the GPU operator shim (make
     ref_gpu_aprod), where the reference tree is mounted; its path, or None."""
-    if not (Path("/root/reference/source/lsqr.c").exists() and shutil.which("gcc")):
+    if not reference_available():
         return None
-    subprocess.run(["make", "-s", "-C", str(HERE), "ref_gpu_aprod", "-j8"], check=True)
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref_gpu_aprod", "-j8", f"REF_SRC={REF_SRC}"],
+                   check=True)
     return REF_GPU_APROD_BIN
 
 
@@ -83,6 +99,9 @@ def lib() -> C.CDLL:
         L.oracle_lsqr.argtypes = [C.POINTER(Problem), C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.c_int, C.c_int, vp, vp, vp, vp,
                                   C.POINTER(Result), C.c_char_p]
+        L.oracle_lsqr_op.argtypes = [C.POINTER(Problem), APROD_FN, vp, C.c_double, C.c_double,
+                                     C.c_double, C.c_double, C.c_int, C.c_int, vp, vp, vp, vp,
+                                     C.POINTER(Result), C.c_char_p]
         L.oracle_set_threads.argtypes = [C.c_int]
         L.oracle_get_threads.restype = C.c_int
         _lib = L
@@ -120,7 +139,11 @@ class OracleProblem:
             raise RuntimeError(f"oracle_aprod failed: {rc}")
 
     def lsqr(self, iterations: int, b_k=None, damp=0.0, atol=1e-10, btol=1e-10, conlim=100.0,
-             itnlim=1000, want_se=False, result_txt=None) -> dict:
+             itnlim=1000, want_se=False, result_txt=None, op=None) -> dict:
+        """The reference's lsqr() (source/lsqr.c:195-917).  op: another
+        operator for it to call in place of the oracle's aprod, a Python
+        callable op(mode, m, n, is_final, iteration) -> int that updates
+        self.y_k / self.y_d (mode 1) or self.x (mode 2) in place."""
         self.y_k[:] = self.prob.b_k if b_k is None else b_k
         self.y_d[:] = 0.0
         n = self.prob.n
@@ -128,9 +151,25 @@ class OracleProblem:
         se = np.zeros(n) if want_se else None
         hist = np.zeros(iterations + 1, ITER_DTYPE)
         r = Result()
-        rc = lib().oracle_lsqr(C.byref(self.c), damp, atol, btol, conlim, itnlim, iterations,
-                               _p(w), _p(x), _p(se), _p(hist), C.byref(r),
-                               result_txt.encode() if result_txt else None)
+        txt = result_txt.encode() if result_txt else None
+        if op is None:
+            rc = lib().oracle_lsqr(C.byref(self.c), damp, atol, btol, conlim, itnlim, iterations,
+                                   _p(w), _p(x), _p(se), _p(hist), C.byref(r), txt)
+        else:
+            errors = []
+
+            def call(mode, m, nn, _prob, _usr, fin, it):
+                try:
+                    return int(op(mode, m, nn, fin, it))
+                except Exception as e:  # stop the solve, re-raised below
+                    errors.append(e)
+                    return 1
+
+            cb = APROD_FN(call)
+            rc = lib().oracle_lsqr_op(C.byref(self.c), cb, None, damp, atol, btol, conlim, itnlim,
+                                      iterations, _p(w), _p(x), _p(se), _p(hist), C.byref(r), txt)
+            if errors:
+                raise errors[0]
         if rc:
             raise RuntimeError(f"oracle_lsqr failed: {rc}")
         res = {k: getattr(r, k) for k, _ in Result._fields_}

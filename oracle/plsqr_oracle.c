@@ -15,6 +15,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -211,11 +212,27 @@ static const char *const msg[6] = {
     "Cond(Abar) seems to be too large, given conlim",
     "The iteration limit was reached"};
 
-/* source/lsqr.c:195-917, one rank */
+/* The built-in operator in the callback's form. */
+static int builtin_aprod(int mode, int m, int n, oracle_problem *p, void *usr, int is_final,
+                         int iteration) {
+  (void)m, (void)n, (void)usr, (void)is_final, (void)iteration;
+  return oracle_aprod(mode, p);
+}
+
 int oracle_lsqr(oracle_problem *p, double damp, double atol, double btol,
                 double conlim, int itnlim, int lsqr_iteration, double *w,
                 double *x, double *se, oracle_iter *hist, oracle_result *res,
                 const char *result_txt) {
+  return oracle_lsqr_op(p, builtin_aprod, NULL, damp, atol, btol, conlim, itnlim,
+                        lsqr_iteration, w, x, se, hist, res, result_txt);
+}
+
+/* source/lsqr.c:195-917, one rank; the operator is called where and as the
+ * reference calls its aprod argument (lsqr.c:366, 491-507, 564) */
+int oracle_lsqr_op(oracle_problem *p, oracle_aprod_fn op, void *usr, double damp,
+                   double atol, double btol, double conlim, int itnlim,
+                   int lsqr_iteration, double *w, double *x, double *se,
+                   oracle_iter *hist, oracle_result *res, const char *result_txt) {
   const int n = p->k_csc.num_col;
   const int num_row = p->k_csc.num_row + p->d_csr.num_row;
   const bool damped = damp > 0.0;
@@ -234,6 +251,7 @@ int oracle_lsqr(oracle_problem *p, double damp, double atol, double btol,
       rhbar1, rhs, rtol, sn, sn1, sn2, t, tau, temp, test1 = 0, test2 = 0,
       test3, theta, t1, t2, t3, xnorm1, z, zbar;
   (void)arnorm0;
+  double loop_seconds = 0.0; /* stays 0 when the start-up ends the solve (:400-401) */
 
   if (nout) fprintf(nout, fmt_1000, enter, num_row, n, damp, (int)wantse, atol,
                     conlim, btol, itnlim);
@@ -250,7 +268,7 @@ int oracle_lsqr(oracle_problem *p, double damp, double atol, double btol,
   beta = dnrm2_forVecY(p); /* :343 */
   if (beta > 0.0) {
     dscal_plsqr3(p, 1.0 / beta); /* :361 */
-    if (oracle_aprod(2, p)) goto fail;
+    if (op(2, num_row, n, p, usr, 0, 0)) goto fail; /* :366 */
     alpha = dnrm2_parallel(n, p->x); /* :375 */
   }
   if (alpha > 0.0) { /* :392-395 */
@@ -280,11 +298,14 @@ int oracle_lsqr(oracle_problem *p, double damp, double atol, double btol,
     fprintf(nout, fmt_1600);
   }
 
+  struct timespec t_loop0, t_loop1; /* :476-478 */
+  clock_gettime(CLOCK_MONOTONIC, &t_loop0);
   if (lsqr_iteration > 0)
     while (1) { /* :480-837 */
       itn = itn + 1;
+      const int last = itn == lsqr_iteration; /* :491-494 */
       dscal_plsqr3(p, -alpha); /* :502 */
-      if (oracle_aprod(1, p)) goto fail; /* :507 */
+      if (op(1, num_row, n, p, usr, last, itn)) goto fail; /* :507 */
       beta = dnrm2_forVecY(p);   /* :516 */
       temp = oracle_d2norm(alpha, beta);
       temp = oracle_d2norm(temp, damp);
@@ -292,7 +313,7 @@ int oracle_lsqr(oracle_problem *p, double damp, double atol, double btol,
       if (beta > 0.0) {
         dscal_plsqr3(p, 1.0 / beta); /* :538 */
         dscal(n, -beta, p->x);       /* :558 */
-        if (oracle_aprod(2, p)) goto fail; /* :564 */
+        if (op(2, num_row, n, p, usr, last, itn)) goto fail; /* :564 */
         alpha = dnrm2_parallel(n, p->x);   /* :577 */
         if (alpha > 0.0) dscal(n, 1.0 / alpha, p->x); /* :595 */
       }
@@ -400,6 +421,9 @@ int oracle_lsqr(oracle_problem *p, double damp, double atol, double btol,
       }
       if (itn == lsqr_iteration) break; /* :833 */
     }
+  clock_gettime(CLOCK_MONOTONIC, &t_loop1); /* :836-842 */
+  loop_seconds =
+      (double)(t_loop1.tv_sec - t_loop0.tv_sec) + 1e-9 * (double)(t_loop1.tv_nsec - t_loop0.tv_nsec);
 
   /* :878-891 */
   if (wantse) {
@@ -423,6 +447,7 @@ goto_800:
     res->istop = istop; res->itn = itn; res->anorm = anorm; res->acond = acond;
     res->rnorm = rnorm; res->arnorm_out = test2; res->xnorm = xnorm;
     res->arnorm = arnorm; res->bnorm = bnorm; res->dxmax = dxmax; res->maxdx = maxdx;
+    res->loop_seconds = loop_seconds;
   }
   return 0;
 

@@ -58,6 +58,9 @@ typedef struct {
   double arnorm; /* alpha*|tau| of the last iteration */
   double bnorm, dxmax;
   int maxdx;
+  /* wall time of the iteration loop, the region of the reference's
+   * "Parallel LSQR time" (source/lsqr.c:476-478, 836-842) */
+  double loop_seconds;
 } oracle_result;
 
 /* source/CPUSpMV.c:162-183  Ax[row_idx[e]] += val[e]*x[col], columns ascending */
@@ -85,6 +88,22 @@ int oracle_lsqr(oracle_problem *p, double damp, double atol, double btol,
                 double conlim, int itnlim, int lsqr_iteration, double *w,
                 double *x, double *se, oracle_iter *hist, oracle_result *res,
                 const char *result_txt);
+
+/* The operator as lsqr() receives it (source/aprod.h:10-13 for one rank:
+ * the version, rank and size arguments dropped, the vectors in p):
+ * mode 1 updates p->y_k / p->y_d with A p->x, mode 2 updates p->x with
+ * A^T [p->y_k; p->y_d]; m, n, isFinalIteration and iteration as lsqr.c
+ * passes them (:366, :491-507, :564).  Returns 0, or non-zero to stop the
+ * solve with an error. */
+typedef int (*oracle_aprod_fn)(int mode, int m, int n, oracle_problem *p, void *usr,
+                               int is_final, int iteration);
+
+/* oracle_lsqr with the operator supplied by the caller (usr is passed
+ * through): the reference's loop driving another implementation of aprod. */
+int oracle_lsqr_op(oracle_problem *p, oracle_aprod_fn op, void *usr, double damp,
+                   double atol, double btol, double conlim, int itnlim,
+                   int lsqr_iteration, double *w, double *x, double *se,
+                   oracle_iter *hist, oracle_result *res, const char *result_txt);
 
 /* Number of OpenMP threads the oracle runs with (0 = OpenMP default). */
 void oracle_set_threads(int nthreads);

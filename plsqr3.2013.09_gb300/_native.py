@@ -21,6 +21,7 @@ ERR = {
     -9: "PLSQR_ERR_INTERNAL", -10: "PLSQR_ERR_NUMERIC",
 }
 PREC_FP64, PREC_MIXED = 0, 1
+ORDER_FAST, ORDER_REFERENCE = 0, 1
 NOALLOC_MAX_ROWS = 1048576  # PLSQR_NOALLOC_MAX_ROWS
 
 vp = C.c_void_p
@@ -41,7 +42,7 @@ class Files(C.Structure):
 
 class Opts(C.Structure):
     _fields_ = [("device", i32), ("precision", i32), ("use_graph", i32), ("verbose", i32),
-                ("grid", i32 * 3), ("pad", i32)]
+                ("grid", i32 * 3), ("order", i32)]
 
 
 class Info(C.Structure):
@@ -67,7 +68,8 @@ class SynthParams(C.Structure):
     _fields_ = [("nx", i32), ("ny", i32), ("nz", i32), ("n_rays", i32), ("tube_radius", f64),
                 ("face_axis", i32), ("n_blobs", i32), ("value_scale", f64), ("blob_sigma", f64),
                 ("checker_amp", f64), ("checker_period", i32), ("pad", i32), ("noise_frac", f64),
-                ("damp_identity", f64), ("damp_lap", f64), ("seed", u64)]
+                ("damp_identity", f64), ("damp_lap", f64), ("damp_cross", f64),
+                ("n_params", i32), ("pad2", i32), ("seed", u64)]
 
 
 class BatchArgs(C.Structure):
@@ -123,6 +125,8 @@ SIGNATURES = {
     "plsqr_write_result": (C.c_int, [vp, C.c_char_p]),
     "plsqr_bench_aprod": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(f64)]),
     "plsqr_bench_iteration": (C.c_int, [vp, C.c_int, C.POINTER(f64)]),
+    "plsqr_set_timing": (C.c_int, [vp, C.c_int]),
+    "plsqr_write_timing": (C.c_int, [vp, C.c_char_p]),
     "plsqr_aprod1_nrm2_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "plsqr_default_batch_args": (None, [C.POINTER(BatchArgs)]),
     "plsqr_batch_variant": (C.c_int, [i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)]),

@@ -15,9 +15,11 @@
 // step between core matrices along K and its stride byte offset the step
 // between 8-row groups.
 //
-// Every wait on an mbarrier is bounded (one second of the global timer); a
-// wait that runs out sets *err, skips the remaining MMAs and the epilogue,
-// and the CTA still frees its tensor memory.
+// Every wait on an mbarrier is bounded (one second of the global timer).  A
+// wait that runs out sets *err; the CTA then writes nothing more into the
+// shared-memory operands (MMAs already issued may still read them), issues
+// no further MMAs, skips the epilogue, waits once more (bounded) for the
+// last commit it issued, and frees its tensor memory.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -158,6 +160,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
   uint64_t *bar = reinterpret_cast<uint64_t *>(wts + S::kWTaps * S::kTapBytes);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
   __shared__ int abort_flag;
+  __shared__ int commits;  // MMA commits issued (written by thread 0 only)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int bxn = (a.g.nx + 7) / 8, byn = (a.g.ny + 15) / 16;
@@ -169,6 +172,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
 
   if (tid == 0) {
     abort_flag = 0;
+    commits = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -230,7 +234,9 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
           abort_flag = 1;
           atomicExch(a.err, 1u);
         }
-        load_taps(s);
+        // after a wait that ran out the MMAs may still read the slots: no
+        // further writes into them
+        if (ok) load_taps(s);
         asm volatile("cp.async.commit_group;" ::: "memory");
       } else {
         asm volatile("cp.async.wait_group 2;" ::: "memory");
@@ -252,11 +258,22 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc2(ConvTcArgs a) {
           tc_mma(tmem, tc_desc(A + kk * 320, 160, S::kLineBytes),
                  tc_desc(B + kk * 256, 128, S::kCoresK * 128), kIdesc, (t > 0 || kk > 0) ? 1u : 0u);
       }
-      if (!kAllW || s == 2) tc_commit(smem_u32(bar));  // phase s (streamed) or 0
+      if (!kAllW || s == 2) {
+        tc_commit(smem_u32(bar));  // phase s (streamed) or 0
+        ++commits;
+      }
     }
   }
-  // the last commit follows every MMA: phase 2 (streamed taps) or 0
-  if (ok && !abort_flag && !mbar_wait(smem_u32(bar), 0u)) ok = false;
+  __syncthreads();
+  if (abort_flag) {
+    // the MMAs already issued may still run: wait (bounded) for the last
+    // commit before the tensor memory is freed
+    ok = false;
+    if (commits > 0) (void)mbar_wait(smem_u32(bar), (uint32_t)((commits - 1) & 1));
+  } else if (ok && !mbar_wait(smem_u32(bar), 0u)) {
+    // the last commit follows every MMA: phase 2 (streamed taps) or 0
+    ok = false;
+  }
   if (!ok) atomicExch(a.err, 1u);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int r = warp * 32 + lane;
@@ -345,6 +362,7 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(GemmTcArgs a) {
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kS * S::kStageBytes);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + kS);
   __shared__ int abort_flag;
+  __shared__ int last_commit;  // step of the last MMA commit issued (thread 0 writes it)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t m0 = (int64_t)blockIdx.x * kTcRows;
@@ -364,6 +382,7 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(GemmTcArgs a) {
 
   if (tid == 0) {
     abort_flag = 0;
+    last_commit = -1;
     for (int s = 0; s < kS; ++s)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -422,7 +441,9 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(GemmTcArgs a) {
     const int tn = t + kS - 1;
     if (tn < steps) {
       if (t >= 1) wait_mma(t - 1);  // stage tn % kS last held step t - 1
-      load(tn, tn % kS);
+      // after a wait that ran out the MMAs may still read the stage: no
+      // further writes into it
+      if (ok) load(tn, tn % kS);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
     asm volatile("cp.async.wait_group %0;" ::"n"(kS - 1) : "memory");
@@ -438,11 +459,15 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(GemmTcArgs a) {
         tc_mma(tmem, tc_desc(A + kk * 256, 128, 1024), tc_desc(B + kk * 256, 128, 1024), kIdesc,
                (t > 0 || kk > 0) ? 1u : 0u);
       tc_commit(smem_u32(&bars[s]));
+      last_commit = t;
     }
   }
-  wait_mma(steps - 1);
+  __syncthreads();
+  if (!abort_flag) wait_mma(steps - 1);
   asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncthreads();
+  if (abort_flag && last_commit >= 0)  // drain (bounded) before the tensor memory is freed
+    (void)mbar_wait(smem_u32(&bars[last_commit % kS]), (uint32_t)((last_commit / kS) & 1));
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   if (!abort_flag) {

@@ -84,9 +84,11 @@ int mixed_prepare(plsqr_ctx *ctx) {
       if (atoi(e) >= 1024 && atoi(e) <= 57344) slab = atoi(e);
     // kernel rows: mostly consecutive columns, read by the lanes of a
     // group in step (transposed chunks); columns: random rows, as stored
+    const int dyn = slab_dyn_blocks(ctx, true);
     if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &M->s_rows,
-                                ctx->slab_group_f)) ||
-        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &M->s_cols)))
+                                ctx->slab_group_f, dyn)) ||
+        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &M->s_cols, 0,
+                                dyn)))
       return rc;
     if ((rc = slab_set_smem<float>(std::max(M->s_rows.smem, M->s_cols.smem)))) return rc;
     M->slabs = true;

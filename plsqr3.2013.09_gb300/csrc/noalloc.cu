@@ -1,24 +1,28 @@
 // plsqr_aprod1_nrm2_noalloc: the kernel-row product y <- y + A x with the
 // 2-norm of the result, for callers that cannot allocate device memory.
 //
-// Who needs it: code that runs inside CUDA stream capture (cudaMalloc is not
-// allowed while a stream is being captured into a graph), code whose device
-// memory is owned by another allocator or a fixed budget (a framework's
-// caching allocator, an MPI rank that sized its buffers up front, the way the
-// reference's driver allocates everything before the solve), and real-time
-// callers that cannot block on the driver's allocator.  They pass every input
-// and output; the only extra memory the product needs, one partial sum of
-// squares per block, lives in a fixed array of this library's module.
+// Who needs it: code whose device memory is owned by another allocator or a
+// fixed budget (a framework's caching allocator, an MPI rank that sized its
+// buffers up front, the way the reference's driver allocates everything
+// before the solve), and real-time callers that cannot block on the driver's
+// allocator (cudaMalloc and cudaFree may synchronise the device).  They pass
+// every input and output; the only extra memory the product needs, one
+// partial sum of squares per block, lives in a fixed array of this library's
+// module.
 //
 // The scratch: `g_noalloc_parts`, kNoAllocParts doubles (128 KB), a static
 // __device__ array.  Every GPU that loads the library holds it until the
 // process exits.  Host code cannot use the array's name as a device address,
 // so the first call on a device, with that device current, looks the address
 // up with cudaGetSymbolAddress and keeps it; make that first call before any
-// stream capture (the lookup may initialise the module).  All calls share the
-// array and every call overwrites the entries it uses, so nothing needs to
-// start at zero, but calls that overlap on the GPU (different streams, no
-// ordering between them) race on it.
+// stream capture (the lookup may initialise the module): a first call on a
+// stream that is being captured is refused with PLSQR_ERR_STATE before it
+// touches the runtime.  The kept address belongs to the device's current
+// context: after cudaDeviceReset in the same process the module is loaded
+// again and the address may change, so calls after a reset are not
+// supported.  All calls share the array and every call overwrites the
+// entries it uses, so nothing needs to start at zero, but calls that overlap
+// on the GPU (different streams, no ordering between them) race on it.
 #include <cuda_runtime.h>
 
 #include <stdint.h>
@@ -89,10 +93,18 @@ extern "C" int plsqr_aprod1_nrm2_noalloc(int32_t n_rows, const int64_t *row_ptr,
     cudaGetLastError();
     return PLSQR_ERR_NODEV;
   }
+  cudaStream_t s = (cudaStream_t)stream;
   double *parts = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mu);
     if (!g_parts_addr[dev]) {
+      // the set-up call must not run while the stream is being captured
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return PLSQR_ERR_CUDA;
+      }
+      if (cap != cudaStreamCaptureStatusNone) return PLSQR_ERR_STATE;
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, g_noalloc_parts) != cudaSuccess || !p) {
         cudaGetLastError();
@@ -102,7 +114,6 @@ extern "C" int plsqr_aprod1_nrm2_noalloc(int32_t n_rows, const int64_t *row_ptr,
     }
     parts = g_parts_addr[dev];
   }
-  cudaStream_t s = (cudaStream_t)stream;
   const int blocks = n_rows > 0 ? (n_rows + kRowsPerBlock - 1) / kRowsPerBlock : 0;
   if (blocks > 0)
     k_noalloc_rows<<<blocks, kThreads, 0, s>>>(n_rows, row_ptr, col_idx, val, x, y, parts);

@@ -9,9 +9,12 @@
  * p_resultx_itn=<K>_NProc=1_float64_mpiio.bin.  -row_ptn, -col_ptn and
  * -col_perm describe a multi-rank partition and are accepted and ignored.
  * Additional options: -precision fp64|mixed, -sweeps S, -inner I, -device G,
- * -quiet, and -x0 FILE: a starting solution for the mixed solver, col raw
+ * -quiet, -x0 FILE: a starting solution for the mixed solver, col raw
  * float64 values (the format of the solution file above), kept where it
- * lowers the residual.
+ * lowers the residual, -order fast|reference: the FP64 sums in parallel order
+ * (default) or in the reference's order (its bits), and -timing FILE: the
+ * iteration timed per region (the reference's GPTL timer names, NVTX
+ * ranges) and written to FILE as JSON.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -28,7 +31,8 @@ int main(int argc, char **argv) {
   const char *damp_i_c = "plsqr3_reorder_small_all.damp.bycol.info.bin";
   const char *damp_f_c = "plsqr3_reorder_small_all.damp.bycol.bin";
   const char *b_k = "vecotrB_ker";
-  const char *x0_path = NULL;
+  const char *x0_path = NULL, *timing_path = NULL;
+  int order = PLSQR_ORDER_FAST;
   int row_k = 10, row_d = 1825, col = 520, itn = 40;
   int precision = PLSQR_PREC_FP64, sweeps = 4, inner = 50, device = 0, verbose = 1;
   for (int i = 1; i < argc; i++) {
@@ -55,6 +59,7 @@ int main(int argc, char **argv) {
     STR("-damp_f_bycol", damp_f_c);
     STR("-b_k", b_k);
     STR("-x0", x0_path);
+    STR("-timing", timing_path);
     INT("-row_k", row_k);
     INT("-row_d", row_d);
     INT("-col", col);
@@ -69,6 +74,11 @@ int main(int argc, char **argv) {
     }
     if (!strcmp(a, "-precision") && v) {
       precision = !strcmp(v, "mixed") ? PLSQR_PREC_MIXED : PLSQR_PREC_FP64;
+      i++;
+      continue;
+    }
+    if (!strcmp(a, "-order") && v) {
+      order = !strcmp(v, "reference") ? PLSQR_ORDER_REFERENCE : PLSQR_ORDER_FAST;
       i++;
       continue;
     }
@@ -96,6 +106,7 @@ int main(int argc, char **argv) {
   o.device = device;
   o.precision = precision;
   o.verbose = verbose && precision == PLSQR_PREC_FP64;
+  o.order = order;
   plsqr_ctx *ctx = NULL;
   int rc = plsqr_ctx_create_files(&f, &o, &ctx);
   if (rc) {
@@ -122,9 +133,14 @@ int main(int argc, char **argv) {
     }
     a.x0 = x0;
   }
+  if (timing_path) plsqr_set_timing(ctx, 1);
   printf("\nStarting plsqr algorithm...procRank=%d\n", 0);
   plsqr_result r;
   rc = plsqr_lsqr(ctx, &a, NULL, NULL, NULL, NULL, NULL, &r);
+  if (rc == PLSQR_OK && timing_path) {
+    const int trc = plsqr_write_timing(ctx, timing_path);
+    if (trc) fprintf(stderr, "plsqr3_gpu: timing report %s: %s\n", timing_path, plsqr_strerror(trc));
+  }
   free(x0);
   if (rc == PLSQR_OK && x0_path) printf("x0 %s\n", r.warm ? "kept" : "not kept (cold start)");
   if (rc) {

@@ -18,6 +18,9 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
+#include "kernels_exact.cuh"
 #include "kernels_fp64.cuh"
 #include "plsqr_internal.h"
 #include "slab.cuh"
@@ -28,6 +31,19 @@ using namespace plsqr;
 namespace {
 
 constexpr int kThreads = 256;
+
+// The regions of one iteration for the timing report and the NVTX ranges,
+// named after the reference's GPTL timers (source/lsqr.c:500-642,
+// aprod_impl.c:69-497); each lists the reference timers whose work it holds
+// (the products fuse the reference's scaling passes into their epilogues).
+constexpr int kRegions = 5;
+const char *const kRegionName[kRegions] = {"spmv", "norm1", "spmvT", "update_x", "krylov_p1"};
+const char *const kRegionCovers[kRegions] = {
+    "scale1 (u *= -alpha), spmv_ker, spmv_damp",
+    "norm1 (beta), scale2 (u *= 1/beta)",
+    "scale1 (v *= -beta), spmvT_ker, spmvT_damp",
+    "norm1 (alpha), scale3 (v *= 1/alpha), krylov_p1 (rotation, x and w update)",
+    "krylov_p1 (dknorm, scalar recurrence, history record)"};
 
 const char *const kErrText[] = {
     "success",
@@ -213,6 +229,19 @@ static void launch_m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
 template <typename T>
 void slab_spmv(const DevSlab<T> &S, int group, const T *x, cudaStream_t s) {
   const SlabCsr<T> A{S.ptr, S.order, S.idx, S.val, S.n_lines, S.n_slabs, S.slab, S.n_idx};
+  if (S.next) {  // persistent form: line counters zeroed, then one block per SM slot
+    cudaMemsetAsync(S.next, 0, sizeof(int) * S.n_slabs, s);
+    const int g = S.dyn_blocks;
+    if (group == 4)
+      k_slab_spmv_dyn<T, 1024, 4><<<g, 1024, S.smem, s>>>(A, S.next, S.chunk, x, S.partial);
+    else if (group == 8)
+      k_slab_spmv_dyn<T, 1024, 8><<<g, 1024, S.smem, s>>>(A, S.next, S.chunk, x, S.partial);
+    else if (group == 32)
+      k_slab_spmv_dyn<T, 1024, 32><<<g, 1024, S.smem, s>>>(A, S.next, S.chunk, x, S.partial);
+    else
+      k_slab_spmv_dyn<T, 1024, 16><<<g, 1024, S.smem, s>>>(A, S.next, S.chunk, x, S.partial);
+    return;
+  }
   const int grid = S.n_slabs * S.bps;
   if (group == 4)
     k_slab_spmv<T, 1024, 4><<<grid, 1024, S.smem, s>>>(A, S.lpart, S.bps, x, S.partial);
@@ -232,7 +261,11 @@ int slab_set_smem(size_t smem) {
   if (cudaFuncSetAttribute(k_slab_spmv<T, 1024, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
       cudaFuncSetAttribute(k_slab_spmv<T, 1024, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
       cudaFuncSetAttribute(k_slab_spmv<T, 1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
-      cudaFuncSetAttribute(k_slab_spmv<T, 1024, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
+      cudaFuncSetAttribute(k_slab_spmv<T, 1024, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
+      cudaFuncSetAttribute(k_slab_spmv_dyn<T, 1024, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
+      cudaFuncSetAttribute(k_slab_spmv_dyn<T, 1024, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
+      cudaFuncSetAttribute(k_slab_spmv_dyn<T, 1024, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ||
+      cudaFuncSetAttribute(k_slab_spmv_dyn<T, 1024, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, b))
     return PLSQR_ERR_CUDA;
   return PLSQR_OK;
 }
@@ -240,6 +273,11 @@ template int slab_set_smem<double>(size_t);
 template int slab_set_smem<float>(size_t);
 
 static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  if (ctx->exact) {  // the reference's order (kernels_exact.cuh); no partial sums
+    k_ref_rows<kThreads><<<ctx->ex_gk + ctx->ex_gd, kThreads, 0, s>>>(
+        ctx->K.csr(), ctx->D.csr(), ctx->v, ctx->u, ctx->ex_gk, mode, ctx->st);
+    return;
+  }
   if (ctx->use_slabs_rows) {
     const DevSlab<double> &S = ctx->s_rows;
     slab_spmv(S, ctx->slab_group, ctx->v, s);
@@ -254,6 +292,11 @@ static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
   }
 }
 static void m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
+  if (ctx->exact) {
+    k_ref_cols<kThreads><<<ctx->ex_gc, kThreads, 0, s>>>(ctx->KC.csr(), ctx->DC.csr(), ctx->u,
+                                                          ctx->m_k, ctx->v, mode, ctx->st);
+    return;
+  }
   if (ctx->use_slabs) {
     const DevSlab<double> &S = ctx->s_cols;
     slab_spmv(S, ctx->slab_group, ctx->u, s);
@@ -274,6 +317,54 @@ static int slab_attrs(plsqr_ctx *ctx) {
   const int rc = slab_set_smem<double>(std::max(ctx->s_rows.smem, ctx->s_cols.smem));
   if (rc) ctx_set_error(ctx, "cudaFuncSetAttribute failed for the slab kernels");
   return rc;
+}
+
+// ---- the reference's order of operations (PLSQR_ORDER_REFERENCE) ----------
+// Scratch of the ordered norms and of the dknorm terms, and the grids of the
+// one-thread-per-line products.
+static int exact_prepare(plsqr_ctx *ctx) {
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  auto chunks = [](int64_t n) { return (int)((n + kNrmChunk - 1) / kNrmChunk); };
+  ctx->ex_nb_k = chunks(ctx->m_k);
+  ctx->ex_nb_d = chunks(ctx->m_d);
+  ctx->ex_nb_v = chunks(ctx->n);
+  const int g = ctx->sm_count * 8;
+  ctx->ex_gk = std::max(1, std::min(g, (ctx->m_k + kThreads - 1) / kThreads));
+  ctx->ex_gd = std::max(1, std::min(g, (ctx->m_d + kThreads - 1) / kThreads));
+  ctx->ex_gc = std::max(1, std::min(g, (ctx->n + kThreads - 1) / kThreads));
+  int rc;
+  if ((rc = dev_alloc(ctx, &ctx->ex_terms, (size_t)std::max<int64_t>(m, ctx->n))) ||
+      (rc = dev_alloc(ctx, &ctx->ex_bmax,
+                      (size_t)std::max(ctx->ex_nb_k + ctx->ex_nb_d, ctx->ex_nb_v))))
+    return rc;
+  return PLSQR_OK;
+}
+
+// beta = ||[y_k; y_d]|| (two segments) or alpha = ||v|| (one)
+static NrmArgs exact_nrm_u(const plsqr_ctx *ctx) {
+  NrmArgs a{};
+  a.nseg = 2;
+  a.bmax = ctx->ex_bmax;
+  a.seg[0] = NrmSeg{ctx->u, ctx->m_k, ctx->ex_terms, 0, ctx->ex_nb_k};
+  a.seg[1] = NrmSeg{ctx->u + ctx->m_k, ctx->m_d, ctx->ex_terms + ctx->m_k, ctx->ex_nb_k,
+                    ctx->ex_nb_d};
+  return a;
+}
+static NrmArgs exact_nrm_v(const plsqr_ctx *ctx) {
+  NrmArgs a{};
+  a.nseg = 1;
+  a.bmax = ctx->ex_bmax;
+  a.seg[0] = NrmSeg{ctx->v, ctx->n, ctx->ex_terms, 0, ctx->ex_nb_v};
+  a.seg[1] = NrmSeg{nullptr, 0, nullptr, ctx->ex_nb_v, 0};
+  return a;
+}
+static void exact_norm(const plsqr_ctx *ctx, const NrmArgs &a, int kind, cudaStream_t s) {
+  const int blocks = a.seg[0].nb + (a.nseg > 1 ? a.seg[1].nb : 0);
+  if (blocks > 0) {
+    k_nrm_max<<<blocks, kNrmThreads, 0, s>>>(a, kind, ctx->st);
+    k_nrm_terms<<<blocks, kNrmThreads, 0, s>>>(a, kind, ctx->st);
+  }
+  k_nrm_chain<<<1, 64, 0, s>>>(a, kind, ctx->st);
 }
 
 // partial-sum counts the norm kernels read
@@ -504,6 +595,8 @@ int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
   plsqr_default_opts(&o);
   if (opts) o = *opts;
   if (ndev < 1 || o.device < 0 || o.device >= ndev) return PLSQR_ERR_NODEV;
+  if (o.order != PLSQR_ORDER_FAST && o.order != PLSQR_ORDER_REFERENCE) return PLSQR_ERR_ARG;
+  if (o.order == PLSQR_ORDER_REFERENCE && o.precision != PLSQR_PREC_FP64) return PLSQR_ERR_ARG;
 
   plsqr_ctx *ctx = new plsqr_ctx();
   ctx->opts = o;
@@ -512,11 +605,12 @@ int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
   ctx->n = n;
   ctx->nnz_k = k_csc->nnz;
   ctx->nnz_d = d_csr->nnz;
+  ctx->exact = o.order == PLSQR_ORDER_REFERENCE;
   if ((rc = ctx_init_common(ctx)) || (rc = upload_lines(ctx, k_csc, kp, &ctx->KC, n)) ||
       (rc = upload_lines(ctx, d_csr, dp, &ctx->D, m_d)) ||
       (rc = upload_lines(ctx, d_csc, dcp, &ctx->DC, n)) || (rc = build_kernel_rows(ctx)) ||
-      (rc = ctx_alloc_vectors(ctx)) || (rc = plan_launch(ctx, kp)) || (rc = slab_plan(ctx)) ||
-      (rc = slab_attrs(ctx))) {
+      (rc = ctx_alloc_vectors(ctx)) || (rc = plan_launch(ctx, kp)) ||
+      (rc = ctx->exact ? exact_prepare(ctx) : slab_plan(ctx)) || (rc = slab_attrs(ctx))) {
     plsqr_ctx_destroy(ctx);
     return rc;
   }
@@ -662,20 +756,80 @@ int plsqr_set_reference_x(plsqr_ctx *ctx, const double *x_ref) {
   return PLSQR_OK;
 }
 
-// Enqueue one LSQR iteration (source/lsqr.c:487-775): five kernels.
-static int enqueue_iteration(plsqr_ctx *ctx, cudaStream_t s) {
+// One LSQR iteration (source/lsqr.c:487-775) as five regions named after
+// the reference's GPTL timers.  Each region is a marker pair: with `ev` (the
+// timed solve) an event is recorded before the first region and after every
+// region, and the host enqueue is bracketed by an NVTX range of the region's
+// name; graph capture and the plain solve pass no events.
+struct Regions {
+  plsqr_ctx *ctx;
+  cudaStream_t s;
+  const cudaEvent_t *ev;
+  int k = 0;
+  void begin() {
+    if (ev) {
+      cudaEventRecord(ev[0], s);
+      nvtxRangePushA(kRegionName[0]);
+    }
+  }
+  void next() {  // end of region k, start of region k + 1
+    if (!ev) return;
+    nvtxRangePop();
+    cudaEventRecord(ev[++k], s);
+    if (k < kRegions) nvtxRangePushA(kRegionName[k]);
+  }
+};
+
+// The reference's order (kernels_exact.cuh): u = -alpha u + A v, beta,
+// u /= beta, v = -beta v + A^T u, alpha, then the rotation, the x/w update
+// and the ordered dknorm sum.
+static int enqueue_iteration_exact(plsqr_ctx *ctx, cudaStream_t s, const cudaEvent_t *ev) {
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
   double *se = ctx->want_se ? ctx->se : nullptr;
   const double *xref = ctx->has_ref ? ctx->xref : nullptr;
+  Regions r{ctx, s, ev};
+  r.begin();
+  m1(ctx, s, kScaleNegAlpha, nullptr);
+  r.next();
+  exact_norm(ctx, exact_nrm_u(ctx), kNrmBeta, s);
+  k_ref_scale_u<kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->st);
+  r.next();
+  m2(ctx, s, kScaleNegBeta, nullptr);
+  r.next();
+  exact_norm(ctx, exact_nrm_v(ctx), kNrmAlpha, s);
+  k_ref_update<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
+      ctx->v, ctx->w, ctx->x, se, xref, ctx->n, ctx->st, ctx->ex_terms,
+      xref ? ctx->parts_err : nullptr, ctx->hist, 0);
+  r.next();
+  k_ref_tail<<<1, 32, 0, s>>>(ctx->st, ctx->ex_terms, ctx->n, xref ? ctx->parts_err : nullptr,
+                              ctx->gvx, ctx->x, ctx->hist);
+  r.next();
+  CK(cudaGetLastError());
+  return PLSQR_OK;
+}
+
+// Enqueue one LSQR iteration: five kernels.
+static int enqueue_iteration(plsqr_ctx *ctx, cudaStream_t s, const cudaEvent_t *ev = nullptr) {
+  if (ctx->exact) return enqueue_iteration_exact(ctx, s, ev);
+  const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
+  double *se = ctx->want_se ? ctx->se : nullptr;
+  const double *xref = ctx->has_ref ? ctx->xref : nullptr;
+  Regions r{ctx, s, ev};
+  r.begin();
   m1(ctx, s, kScaleNegAlpha, ctx->parts_u);
+  r.next();
   k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->parts_u, ctx_pu_k(ctx),
                                                              ctx_pu_d(ctx), ctx->st, 0);
+  r.next();
   m2(ctx, s, kScaleNegBeta, ctx->parts_v);
+  r.next();
   k_update_x<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
       ctx->v, ctx->w, ctx->x, se, xref, ctx->n, ctx->parts_v, ctx_pv(ctx), ctx->st, ctx->parts_dk,
       xref ? ctx->parts_err : nullptr, ctx->hist, 0);
+  r.next();
   k_tail<kThreads><<<1, kThreads, 0, s>>>(ctx->st, ctx->parts_dk, xref ? ctx->parts_err : nullptr,
                                            ctx->gvx, ctx->x, ctx->hist);
+  r.next();
   CK(cudaGetLastError());
   return PLSQR_OK;
 }
@@ -751,26 +905,53 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
   if (ctx->has_ref) k_ref_norm<kThreads><<<1, kThreads, 0, ctx->stream>>>(ctx->xref, ctx->n, ctx->st);
 
   // start-up: beta u = b, alpha v = A^T u (lsqr.c:343-445)
+  nvtxRangePushA("norm0+spmvT_init");
   CK(cudaEventRecord(ctx->ev_start, ctx->stream));
   const int64_t m = (int64_t)ctx->m_k + ctx->m_d;
-  k_sumsq_u<kThreads><<<ctx->gsk + ctx->gsd, kThreads, 0, ctx->stream>>>(ctx->u, ctx->m_k, ctx->m_d,
-                                                                          ctx->gsk, ctx->parts_u);
-  k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, ctx->parts_u, ctx->gsk,
-                                                              ctx->gsd, ctx->st, 1);
-  if ((rc = launch_aprod(ctx, 2, kScaleZero, true))) return rc;
-  k_update_x<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
-      ctx->v, ctx->w, ctx->x, ctx->want_se ? ctx->se : nullptr, nullptr, ctx->n, ctx->parts_v,
-      ctx_pv(ctx), ctx->st, ctx->parts_dk, nullptr, ctx->hist, 1);
+  if (ctx->exact) {
+    exact_norm(ctx, exact_nrm_u(ctx), kNrmBetaStart, ctx->stream);
+    k_ref_scale_u<kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(ctx->u, m, ctx->st);
+    if ((rc = launch_aprod(ctx, 2, kScaleZero, false))) return rc;
+    exact_norm(ctx, exact_nrm_v(ctx), kNrmAlpha, ctx->stream);
+    k_ref_update<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
+        ctx->v, ctx->w, ctx->x, ctx->want_se ? ctx->se : nullptr, nullptr, ctx->n, ctx->st,
+        ctx->ex_terms, nullptr, ctx->hist, 1);
+  } else {
+    k_sumsq_u<kThreads><<<ctx->gsk + ctx->gsd, kThreads, 0, ctx->stream>>>(
+        ctx->u, ctx->m_k, ctx->m_d, ctx->gsk, ctx->parts_u);
+    k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(
+        ctx->u, m, ctx->parts_u, ctx->gsk, ctx->gsd, ctx->st, 1);
+    if ((rc = launch_aprod(ctx, 2, kScaleZero, true))) return rc;
+    k_update_x<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
+        ctx->v, ctx->w, ctx->x, ctx->want_se ? ctx->se : nullptr, nullptr, ctx->n, ctx->parts_v,
+        ctx_pv(ctx), ctx->st, ctx->parts_dk, nullptr, ctx->hist, 1);
+  }
   CK(cudaGetLastError());
   DevState cur;
   CK(cudaMemcpyAsync(&cur, ctx->st, sizeof(cur), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  nvtxRangePop();
 
   int done_itn = 0;
   float ms = 0.f, ms_total = 0.f;
+  // timed solve: events around every region of every iteration, no graph
+  const bool timed = ctx->timing;
+  std::vector<cudaEvent_t> evs;
+  struct EventPool {
+    std::vector<cudaEvent_t> &e;
+    ~EventPool() {
+      for (cudaEvent_t x : e) cudaEventDestroy(x);
+    }
+  } pool{evs};
+  if (timed) {
+    ctx->t_iters = 0;
+    evs.assign((size_t)itn * (kRegions + 1), nullptr);
+    for (auto &e : evs) CK(cudaEventCreate(&e));
+  }
   if (!cur.done && itn > 0) {
-    const bool graph = ctx->opts.use_graph != 0;
+    const bool graph = ctx->opts.use_graph != 0 && !timed;
     if (graph && (rc = ensure_graph(ctx))) return rc;
+    nvtxRangePushA("LSQR_MAIN_ITERATION");
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
     const int chunk = args->stop_on_istop ? 10 : itn;
     while (done_itn < itn) {
@@ -778,7 +959,9 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
       for (int i = 0; i < k; ++i) {
         if (graph)
           CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-        else if ((rc = enqueue_iteration(ctx, ctx->stream)))
+        else if ((rc = enqueue_iteration(
+                      ctx, ctx->stream,
+                      timed ? evs.data() + (size_t)(done_itn + i) * (kRegions + 1) : nullptr)))
           return rc;
       }
       done_itn += k;
@@ -790,8 +973,20 @@ int plsqr_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     }
     CK(cudaEventRecord(ctx->ev1, ctx->stream));
     CK(cudaEventSynchronize(ctx->ev1));
+    nvtxRangePop();
     CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     CK(cudaEventElapsedTime(&ms_total, ctx->ev_start, ctx->ev1));
+  }
+  if (timed) {
+    ctx->t_ms.assign((size_t)done_itn * kRegions, 0.f);
+    for (int i = 0; i < done_itn; ++i)
+      for (int r = 0; r < kRegions; ++r)
+        CK(cudaEventElapsedTime(&ctx->t_ms[(size_t)i * kRegions + r],
+                                evs[(size_t)i * (kRegions + 1) + r],
+                                evs[(size_t)i * (kRegions + 1) + r + 1]));
+    ctx->t_iters = done_itn;
+    ctx->t_loop_ms = ms;
+    ctx->t_startup_ms = ms_total - ms;
   }
   if (ctx->want_se && done_itn > 0)
     k_finish_se<<<ctx->gvx, kThreads, 0, ctx->stream>>>(ctx->se, ctx->n, ctx->st, ctx->m_k + ctx->m_d);
@@ -878,6 +1073,47 @@ int plsqr_bench_iteration(plsqr_ctx *ctx, int reps, double *ms_per_iteration) {
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   *ms_per_iteration = (double)ms / reps;
   return PLSQR_OK;
+}
+
+int plsqr_set_timing(plsqr_ctx *ctx, int on) {
+  if (!ctx) return PLSQR_ERR_ARG;
+  ctx->timing = on != 0;
+  return PLSQR_OK;
+}
+
+int plsqr_write_timing(const plsqr_ctx *ctx, const char *path) {
+  if (!ctx || !path) return PLSQR_ERR_ARG;
+  if (ctx->t_iters <= 0) return PLSQR_ERR_STATE;
+  FILE *f = fopen(path, "w");
+  if (!f) return PLSQR_ERR_IO;
+  const int n = ctx->t_iters;
+  fprintf(f, "{\n \"timer\": \"CUDA events on the context's stream around each region\",\n");
+  fprintf(f, " \"order\": \"%s\",\n \"iterations\": %d,\n", ctx->exact ? "reference" : "fast", n);
+  fprintf(f, " \"LSQR_MAIN_ITERATION\": {\"seconds\": %.9g},\n", 1e-3 * ctx->t_loop_ms);
+  fprintf(f, " \"startup_seconds\": %.9g,\n \"regions\": [\n", 1e-3 * ctx->t_startup_ms);
+  for (int r = 0; r < kRegions; ++r) {
+    double sum = 0.0, mn = 1e300, mx = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double t = ctx->t_ms[(size_t)i * kRegions + r];
+      sum += t;
+      mn = std::min(mn, t);
+      mx = std::max(mx, t);
+    }
+    fprintf(f,
+            "  {\"name\": \"%s\", \"covers\": \"%s\", \"seconds\": %.9g, "
+            "\"ms_per_iteration\": %.6g, \"min_ms\": %.6g, \"max_ms\": %.6g}%s\n",
+            kRegionName[r], kRegionCovers[r], 1e-3 * sum, sum / n, mn, mx,
+            r + 1 < kRegions ? "," : "");
+  }
+  fprintf(f, " ],\n \"per_iteration_ms\": {\n");
+  for (int r = 0; r < kRegions; ++r) {
+    fprintf(f, "  \"%s\": [", kRegionName[r]);
+    for (int i = 0; i < n; ++i)
+      fprintf(f, "%s%.5g", i ? ", " : "", (double)ctx->t_ms[(size_t)i * kRegions + r]);
+    fprintf(f, "]%s\n", r + 1 < kRegions ? "," : "");
+  }
+  fprintf(f, " }\n}\n");
+  return fclose(f) == 0 ? PLSQR_OK : PLSQR_ERR_IO;
 }
 
 int plsqr_get_x(plsqr_ctx *ctx, double *x) {

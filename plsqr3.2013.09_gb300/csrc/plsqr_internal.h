@@ -32,6 +32,11 @@ struct DevSlab {
   int bps = 0;               // blocks per slab
   T *partial = nullptr;      // [n_slabs * n_lines]
   size_t smem = 0;           // shared memory per block
+  // persistent form (k_slab_spmv_dyn): per-slab line counters, or null for
+  // the static block-per-range form; its grid
+  int *next = nullptr;
+  int dyn_blocks = 0;
+  int chunk = 4;  // passes of lines a warp takes per counter grab
 };
 
 struct MixedState;  // mixed.cu
@@ -73,6 +78,17 @@ struct plsqr_ctx {
   int gc1k = 1, gc1d = 1, gc2 = 1;  // grids of the combine kernels
   BatchState *batch = nullptr;       // several right-hand sides (batched.cu)
   double *d_val0 = nullptr, *dc_val0 = nullptr;  // damping values before weighting
+  // PLSQR_ORDER_REFERENCE: the reference's order of operations (kernels_exact.cuh)
+  bool exact = false;
+  double *ex_terms = nullptr;  // [max(m, n)] norm and dknorm terms
+  double *ex_bmax = nullptr;   // per-chunk maxima of the norm passes
+  int ex_nb_k = 0, ex_nb_d = 0, ex_nb_v = 0;  // norm-pass blocks of y_k, y_d, v
+  int ex_gk = 1, ex_gd = 1, ex_gc = 1;        // grids of the product kernels
+  // timing report (plsqr_set_timing / plsqr_write_timing)
+  bool timing = false;
+  std::vector<float> t_ms;  // [iterations][regions] device time of each region
+  int t_iters = 0;          // iterations of the last timed solve (0: none)
+  float t_loop_ms = 0.f, t_startup_ms = 0.f;
 };
 
 // plsqr_gpu.cu: PLSQR_ERR_NUMERIC for NaN, Inf, or a largest magnitude
@@ -83,8 +99,14 @@ int magnitude_ok(const double *p, int64_t n, int allow_small = 0);
 template <typename T>
 // tgroup > 1: transpose each segment's chunks for products that stream it
 // with tgroup lanes (slab_pos in slab.cuh); 0 keeps the order
+// dyn_blocks > 0: the persistent form with that many blocks (one range per
+// slab, the whole slab in longest-segment-first order); 0: the static form
 int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, int blocks,
-               DevSlab<T> *out, int tgroup = 0);
+               DevSlab<T> *out, int tgroup = 0, int dyn_blocks = 0);
+// The scheduling of the slab products from the environment: PLSQR_SLAB_SCHED
+// (FP64) or PLSQR_SLAB_SCHED_F (FP32), 1 persistent, 0 static; returns the
+// persistent grid or 0.
+int slab_dyn_blocks(const plsqr_ctx *ctx, bool fp32);
 int slab_plan(plsqr_ctx *ctx);
 // plsqr_gpu.cu: slab product launch and its shared-memory attribute
 template <typename T>

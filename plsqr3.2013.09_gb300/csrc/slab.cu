@@ -26,9 +26,19 @@ namespace {
 constexpr int kMaxSlabs = 64;  // k_slab_count / k_slab_fill keep one counter per slab
 }
 
+int slab_dyn_blocks(const plsqr_ctx *ctx, bool fp32) {
+  // defaults measured on the 96x96x32 problem: the FP64 A^T y product
+  // 2.81 -> 2.66 ms persistent; the FP32 products slower persistent
+  int on = fp32 ? 0 : 1;
+  if (const char *e = getenv(fp32 ? "PLSQR_SLAB_SCHED_F" : "PLSQR_SLAB_SCHED"))
+    if (e[0] == '0' || e[0] == '1') on = e[0] - '0';
+  // resident blocks per SM: one 192 KB FP64 slab, two 96 KB FP32 slabs
+  return on ? ctx->sm_count * (fp32 ? 2 : 1) : 0;
+}
+
 template <typename T>
 int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, int blocks,
-               DevSlab<T> *out, int tgroup) {
+               DevSlab<T> *out, int tgroup, int dyn_blocks) {
   const int n_lines = L.n_lines;
   const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
   if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
@@ -72,6 +82,14 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, i
   int bps = std::max(1, (blocks + n_slabs - 1) / n_slabs);
   if (const char *e = getenv("PLSQR_SLAB_BLOCKS"))
     if (atoi(e) > 0) bps = std::max(1, atoi(e) / n_slabs);
+  if (dyn_blocks > 0) {  // persistent form: one range, the whole slab sorted
+    bps = 1;
+    out->dyn_blocks = dyn_blocks;
+    out->chunk = 4;
+    if (const char *e = getenv("PLSQR_SLAB_CHUNK"))
+      if (atoi(e) >= 1 && atoi(e) <= 64) out->chunk = atoi(e);
+    if ((rc = dev_alloc(ctx, &out->next, (size_t)n_slabs))) return rc;
+  }
   out->bps = bps;
   std::vector<int32_t> lp((size_t)n_slabs * (bps + 1));
   for (int s = 0; s < n_slabs; ++s) {
@@ -108,9 +126,9 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, i
 }
 
 template int build_slab<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t, int,
-                                DevSlab<double> *, int);
+                                DevSlab<double> *, int, int);
 template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, int,
-                               DevSlab<float> *, int);
+                               DevSlab<float> *, int, int);
 
 // Plan the slab paths.  slab_ok: every dimension fits kMaxSlabs slabs of
 // 24,576 FP32 values, so the mixed solver's inner products use FP32 slabs.
@@ -138,11 +156,15 @@ int slab_plan(plsqr_ctx *ctx) {
   if (ctx->nnz_k == 0 || mode <= 0) return PLSQR_OK;
   int rc;
   if (mode == 1 && rows_fit) {
-    if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &ctx->s_rows))) return rc;
+    if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &ctx->s_rows, 0,
+                                 slab_dyn_blocks(ctx, false))))
+      return rc;
     ctx->use_slabs_rows = true;
   }
   if ((mode == 1 || mode == 2) && cols_fit) {
-    if ((rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &ctx->s_cols))) return rc;
+    if ((rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &ctx->s_cols, 0,
+                                 slab_dyn_blocks(ctx, false))))
+      return rc;
     ctx->use_slabs = true;
   }
   return PLSQR_OK;

@@ -208,6 +208,106 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
   }
 }
 
+// The same product as a persistent kernel: one block per SM slot; blocks
+// take lines of a slab from the slab's counter in next[] (chunk * 32 / kGroup
+// consecutive lines per warp and grab, a group's line per pass, in the slab's
+// longest-segment-first order, A.order with one range per slab), so that
+// every warp stays busy until the slab runs out; the block then stages the next slab that still has lines (counters
+// shared by all blocks, so fast SMs take over the work of slow ones) and
+// passes each slab once.  next[] is zeroed before every launch.  A
+// segment's partial comes from one group whichever block takes it, with the
+// same lanes and order: the results equal the static kernel's bit for bit.
+template <typename T, int kThreads, int kGroup>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 2 : 1)
+    k_slab_spmv_dyn(SlabCsr<T> A, int *__restrict__ next, int chunk, const T *__restrict__ x,
+                    T *__restrict__ partial) {
+  static_assert(kGroup == 4 || kGroup == 8 || kGroup == 16 || kGroup == 32, "4 to 32 lanes");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *xs = reinterpret_cast<T *>(smem_raw);
+  __shared__ int s_left;
+  constexpr int kPerWarp = 32 / kGroup;
+  const int lane = threadIdx.x & 31;
+  const int sub = threadIdx.x & (kGroup - 1);
+  const int gw = lane / kGroup;  // group within the warp
+  const uint4 *idx8 = reinterpret_cast<const uint4 *>(A.idx);
+  int s = (int)(((int64_t)blockIdx.x * A.n_slabs) / gridDim.x);
+  for (int visit = 0; visit < A.n_slabs; ++visit, s = (s + 1 == A.n_slabs) ? 0 : s + 1) {
+    if (threadIdx.x == 0) s_left = *reinterpret_cast<volatile int *>(next + s) < A.n_lines;
+    __syncthreads();
+    const bool left = s_left;  // the same decision in every thread of the block
+    __syncthreads();           // read before thread 0 writes the next slab's
+    if (!left) continue;
+    const int64_t base = (int64_t)s * A.slab;
+    const int len = (int)min((int64_t)A.slab, (int64_t)A.n_idx - base);
+    for (int i = threadIdx.x; i < len; i += kThreads) xs[i] = x[base + i];
+    __syncthreads();
+    const int64_t *ptr = A.ptr + (int64_t)s * (A.n_lines + 1);
+    const int32_t *order = A.order + (int64_t)s * A.n_lines;
+    int k0 = 0, c = chunk;  // this warp's grab: lines [k0, k0 + chunk * kPerWarp)
+    for (;;) {
+      if (c == chunk) {
+        if (lane == 0) k0 = atomicAdd(next + s, chunk * kPerWarp);
+        k0 = __shfl_sync(0xffffffffu, k0, 0);
+        c = 0;
+      }
+      if (k0 >= A.n_lines) break;
+      const int k = k0 + gw;
+      k0 += kPerWarp;
+      ++c;
+      const int l = k < A.n_lines ? order[k] : 0;
+      T acc0 = 0, acc1 = 0;
+      if (k < A.n_lines) {
+        const int64_t g0 = ptr[l] >> 3, g1 = ptr[l + 1] >> 3;
+        int64_t g = g0 + sub;
+        for (; g + kGroup < g1; g += 2 * kGroup) {
+          if (g + 4 * kGroup < g1) {
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(idx8 + g + 4 * kGroup));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(A.val + (g + 4 * kGroup) * 8));
+          }
+          const uint4 q = __ldg(idx8 + g), p = __ldg(idx8 + g + kGroup);
+          T v[8], w[8];
+          load8(A.val, g, v);
+          load8(A.val, g + kGroup, w);
+          acc0 = fmaT(v[0], xs[q.x & 0xffff], acc0);
+          acc1 = fmaT(v[1], xs[q.x >> 16], acc1);
+          acc0 = fmaT(v[2], xs[q.y & 0xffff], acc0);
+          acc1 = fmaT(v[3], xs[q.y >> 16], acc1);
+          acc0 = fmaT(v[4], xs[q.z & 0xffff], acc0);
+          acc1 = fmaT(v[5], xs[q.z >> 16], acc1);
+          acc0 = fmaT(v[6], xs[q.w & 0xffff], acc0);
+          acc1 = fmaT(v[7], xs[q.w >> 16], acc1);
+          acc0 = fmaT(w[0], xs[p.x & 0xffff], acc0);
+          acc1 = fmaT(w[1], xs[p.x >> 16], acc1);
+          acc0 = fmaT(w[2], xs[p.y & 0xffff], acc0);
+          acc1 = fmaT(w[3], xs[p.y >> 16], acc1);
+          acc0 = fmaT(w[4], xs[p.z & 0xffff], acc0);
+          acc1 = fmaT(w[5], xs[p.z >> 16], acc1);
+          acc0 = fmaT(w[6], xs[p.w & 0xffff], acc0);
+          acc1 = fmaT(w[7], xs[p.w >> 16], acc1);
+        }
+        for (; g < g1; g += kGroup) {
+          const uint4 q = __ldg(idx8 + g);
+          T v[8];
+          load8(A.val, g, v);
+          acc0 = fmaT(v[0], xs[q.x & 0xffff], acc0);
+          acc1 = fmaT(v[1], xs[q.x >> 16], acc1);
+          acc0 = fmaT(v[2], xs[q.y & 0xffff], acc0);
+          acc1 = fmaT(v[3], xs[q.y >> 16], acc1);
+          acc0 = fmaT(v[4], xs[q.z & 0xffff], acc0);
+          acc1 = fmaT(v[5], xs[q.z >> 16], acc1);
+          acc0 = fmaT(v[6], xs[q.w & 0xffff], acc0);
+          acc1 = fmaT(v[7], xs[q.w >> 16], acc1);
+        }
+      }
+      T t = acc0 + acc1;
+#pragma unroll
+      for (int o = kGroup / 2; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (sub == 0 && k < A.n_lines) partial[(int64_t)s * A.n_lines + l] = t;
+    }
+    __syncthreads();  // every warp is done with xs before the next slab is staged
+  }
+}
+
 // u_k[r] = scale*u_k[r] + sum_s partial[s][r] (blocks [0, gk)); u_d[r] =
 // scale*u_d[r] + (D v)[r] (blocks [gk, grid)); per-block sums of squares.
 // P: type of the slab partials, T: type of the vectors (the mixed solver

@@ -7,10 +7,13 @@
 //    on the two opposite grid faces normal to `face_axis`; its nonzeros are the
 //    cells whose centre lies within `tube_radius` of the segment, each valued
 //    |N(0,1)| * value_scale.  Columns of a row are ascending.
-//  * Damping matrix D, rows in the per-cell order of damping_binary.py:84-511
-//    with the cross terms left out: identity row (weight damp_identity), then
-//    the forward 1,-2,1 second difference along x, y, z (weight damp_lap) when
-//    the stencil fits in the grid.
+//  * Damping matrix D, rows in the per-cell order of damping_binary.py:84-511:
+//    identity row (weight damp_identity), the forward 1,-2,1 second difference
+//    along x, y, z (weight damp_lap), and, when damp_cross != 0, the cross
+//    differences 0.5 * (1, -1, -1, 1) over the corners (0,0), (2,0), (0,2),
+//    (2,2) of the xy, xz and yz planes (weight damp_cross); a row only where
+//    its stencil fits in the grid.  With n_params fields the whole block
+//    repeats per field (damping_binary.py:84, 578-610).
 //  * x_true: Gaussian blobs (centre uniform in the grid, amplitude N(0,1)) plus
 //    an optional +-checker_amp checkerboard of period checker_period cells.
 //  * b_k = K x_true + noise_frac * rms(K x_true) * N(0,1).
@@ -260,20 +263,43 @@ int plsqr_synth_kernel_fill(const plsqr_synth_params *P, const int64_t *row_ptr,
   return bad ? PLSQR_ERR_INTERNAL : 0;
 }
 
-// Rows per cell in damping_binary.py order (identity, xx, yy, zz).
-static inline int damp_rows_of_cell(const plsqr_synth_params *P, int ix, int iy, int iz) {
-  return 1 + (ix < P->nx - 2) + (iy < P->ny - 2) + (iz < P->nz - 2);
+// Rows and nonzeros of one cell's damping rows, in damping_binary.py's order:
+// identity, xx, yy, zz, then (damp_cross != 0) xy, xz, yz.
+struct CellRows {
+  int fx, fy, fz, fxy, fxz, fyz;
+  int rows() const { return 1 + fx + fy + fz + fxy + fxz + fyz; }
+  int nnz() const { return 1 + 3 * (fx + fy + fz) + 4 * (fxy + fxz + fyz); }
+};
+static inline CellRows cell_rows(const plsqr_synth_params *P, int ix, int iy, int iz) {
+  CellRows c;
+  c.fx = ix < P->nx - 2;
+  c.fy = iy < P->ny - 2;
+  c.fz = iz < P->nz - 2;
+  const int cr = P->damp_cross != 0.0;
+  c.fxy = cr && c.fx && c.fy;
+  c.fxz = cr && c.fx && c.fz;
+  c.fyz = cr && c.fy && c.fz;
+  return c;
+}
+static inline int n_fields(const plsqr_synth_params *P) {
+  return P->n_params > 1 ? P->n_params : 1;
 }
 
 int plsqr_synth_damping_size(const plsqr_synth_params *P, int64_t *m_d, int64_t *nnz_d) {
   int rc = check_params(P);
   if (rc) return rc;
-  const int64_t n = (int64_t)P->nx * P->ny * P->nz;
-  const int64_t lx = (int64_t)std::max(0, P->nx - 2) * P->ny * P->nz;
-  const int64_t ly = (int64_t)P->nx * std::max(0, P->ny - 2) * P->nz;
-  const int64_t lz = (int64_t)P->nx * P->ny * std::max(0, P->nz - 2);
-  *m_d = n + lx + ly + lz;
-  *nnz_d = n + 3 * (lx + ly + lz);
+  const int64_t nx = P->nx, ny = P->ny, nz = P->nz, n = nx * ny * nz;
+  const int64_t ex = std::max<int64_t>(0, nx - 2), ey = std::max<int64_t>(0, ny - 2),
+                ez = std::max<int64_t>(0, nz - 2);
+  const int64_t lx = ex * ny * nz, ly = nx * ey * nz, lz = nx * ny * ez;
+  int64_t rows = n + lx + ly + lz, nnz = n + 3 * (lx + ly + lz);
+  if (P->damp_cross != 0.0) {
+    const int64_t cxy = ex * ey * nz, cxz = ex * ny * ez, cyz = nx * ey * ez;
+    rows += cxy + cxz + cyz;
+    nnz += 4 * (cxy + cxz + cyz);
+  }
+  *m_d = rows * n_fields(P);
+  *nnz_d = nnz * n_fields(P);
   return 0;
 }
 
@@ -283,39 +309,49 @@ int plsqr_synth_damping_fill(const plsqr_synth_params *P, int64_t *row_ptr,
   if (rc) return rc;
   const int nx = P->nx, ny = P->ny, nz = P->nz;
   const int64_t ncell = (int64_t)nx * ny * nz;
-  // first row and first nonzero of every cell, by a prefix over cells
-  std::vector<int64_t> row0(ncell + 1);
-  row0[0] = 0;
+  // first row and first nonzero of every cell of field 0, by a prefix over cells
+  std::vector<int64_t> row0(ncell + 1), nz0(ncell + 1);
+  row0[0] = nz0[0] = 0;
   for (int64_t c = 0; c < ncell; ++c) {
     const int ix = (int)(c % nx), iy = (int)((c / nx) % ny), iz = (int)(c / ((int64_t)nx * ny));
-    row0[c + 1] = row0[c] + damp_rows_of_cell(P, ix, iy, iz);
+    const CellRows cr = cell_rows(P, ix, iy, iz);
+    row0[c + 1] = row0[c] + cr.rows();
+    nz0[c + 1] = nz0[c] + cr.nnz();
   }
+  const int64_t rows_f = row0[ncell], nnz_f = nz0[ncell];
+  const int64_t sx = 1, sy = nx, sz = (int64_t)nx * ny;
   row_ptr[0] = 0;
+  for (int f = 0; f < n_fields(P); ++f) {
 #pragma omp parallel for schedule(static)
-  for (int64_t c = 0; c < ncell; ++c) {
-    const int ix = (int)(c % nx), iy = (int)((c / nx) % ny), iz = (int)(c / ((int64_t)nx * ny));
-    int64_t r = row0[c];
-    // nonzeros before this cell's first row: one per identity row (c of them)
-    // plus three per stencil row (row0[c] - c of them)
-    int64_t e = row0[c] + 2 * (row0[c] - c);
-    // identity
-    col_idx[e] = (int32_t)c;
-    val[e] = P->damp_identity;
-    row_ptr[r + 1] = e + 1;
-    ++r;
-    ++e;
-    const int64_t strides[3] = {1, nx, (int64_t)nx * ny};
-    const int fits[3] = {ix < nx - 2, iy < ny - 2, iz < nz - 2};
-    for (int a = 0; a < 3; ++a) {
-      if (!fits[a]) continue;
-      const double w[3] = {1.0, -2.0, 1.0};
-      for (int j = 0; j < 3; ++j) {
-        col_idx[e + j] = (int32_t)(c + j * strides[a]);
-        val[e + j] = w[j] * P->damp_lap;
-      }
-      e += 3;
-      row_ptr[r + 1] = e;
-      ++r;
+    for (int64_t c = 0; c < ncell; ++c) {
+      const int ix = (int)(c % nx), iy = (int)((c / nx) % ny), iz = (int)(c / ((int64_t)nx * ny));
+      const CellRows cr = cell_rows(P, ix, iy, iz);
+      const int64_t col0 = c + f * ncell;
+      int64_t r = row0[c] + f * rows_f, e = nz0[c] + f * nnz_f;
+      auto row = [&](int k, const int64_t *off, const double *w, double weight) {
+        for (int j = 0; j < k; ++j) {
+          col_idx[e + j] = (int32_t)(col0 + off[j]);
+          val[e + j] = w[j] * weight;
+        }
+        e += k;
+        row_ptr[r + 1] = e;
+        ++r;
+      };
+      const int64_t id[1] = {0};
+      const double one[1] = {1.0};
+      row(1, id, one, P->damp_identity);
+      const double lap[3] = {1.0, -2.0, 1.0};
+      const int64_t ox[3] = {0, sx, 2 * sx}, oy[3] = {0, sy, 2 * sy}, oz[3] = {0, sz, 2 * sz};
+      if (cr.fx) row(3, ox, lap, P->damp_lap);
+      if (cr.fy) row(3, oy, lap, P->damp_lap);
+      if (cr.fz) row(3, oz, lap, P->damp_lap);
+      const double crs[4] = {0.5, -0.5, -0.5, 0.5};
+      const int64_t oxy[4] = {0, 2 * sx, 2 * sy, 2 * sx + 2 * sy};
+      const int64_t oxz[4] = {0, 2 * sx, 2 * sz, 2 * sx + 2 * sz};
+      const int64_t oyz[4] = {0, 2 * sy, 2 * sz, 2 * sy + 2 * sz};
+      if (cr.fxy) row(4, oxy, crs, P->damp_cross);
+      if (cr.fxz) row(4, oxz, crs, P->damp_cross);
+      if (cr.fyz) row(4, oyz, crs, P->damp_cross);
     }
   }
   return 0;

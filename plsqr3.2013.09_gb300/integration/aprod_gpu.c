@@ -9,8 +9,11 @@
  * first call builds a GPU context from the matrices in PPDataV3_TRI (K by
  * column, D by row and by column, main.h:246-251, 414); every call then copies
  * the input vector to the device and the updated one back, as the reference's
- * own GPU wrappers did around each product (aprod_impl.c:116-119, 154, 190);
- * the final iteration releases the context.  Errors end the run through
+ * own GPU wrappers did around each product (aprod_impl.c:116-119, 154, 190).
+ * lsqr.c passes isFinalIteration = 1 to both calls of its last iteration
+ * (:491-507, :564); the context is released by the second of them, the
+ * mode-2 call, or at exit where that call does not come (beta = 0 in the
+ * last iteration skips it, lsqr.c:530).  Errors end the run through
  * MPI_Abort, as the reference's aprod does on its own failures.
  */
 #include <stdio.h>
@@ -25,6 +28,11 @@ typedef char aprod_gpu_needs_fp64[sizeof(MY_FLOAT_TYPE) == sizeof(double) ? 1 : 
 
 static plsqr_ctx *g_ctx;
 
+static void release_ctx(void) {
+  plsqr_ctx_destroy(g_ctx);
+  g_ctx = NULL;
+}
+
 static int make_ctx(PPDataV3_TRI *p) {
   const SpMatCSC *k = p->matCSC_k;
   const SpMatCSR *d = p->matCSR_d;
@@ -33,7 +41,11 @@ static int make_ctx(PPDataV3_TRI *p) {
   plsqr_sparse ds = {d->numRow, d->numCol, d->numNonzero, d->row_ptr, NULL, d->col_idx, d->val};
   plsqr_sparse dcs = {dc->numRow, dc->numCol, dc->numNonzero, dc->col_ptr, NULL, dc->row_idx,
                       dc->val};
-  return plsqr_ctx_create(&ks, &ds, &dcs, NULL, &g_ctx);
+  static int at_exit;
+  const int rc = plsqr_ctx_create(&ks, &ds, &dcs, NULL, &g_ctx);
+  /* registered after the CUDA runtime has started, so that it runs first */
+  if (rc == PLSQR_OK && !at_exit) at_exit = atexit(release_ctx) == 0;
+  return rc;
 }
 
 void aprod(int version, int procRank, int numProc, int mode, int m, int n, MY_FLOAT_TYPE x[],
@@ -53,8 +65,5 @@ void aprod(int version, int procRank, int numProc, int mode, int m, int n, MY_FL
     fprintf(stderr, "aprod on GPU: %s\n", plsqr_strerror(rc));
     MPI_Abort(MPI_COMM_WORLD, 1);
   }
-  if (isFinalIteration) {
-    plsqr_ctx_destroy(g_ctx);
-    g_ctx = NULL;
-  }
+  if (isFinalIteration && mode == 2) release_ctx();
 }

@@ -31,7 +31,7 @@ def _f64(a, n, name):
 class Context:
     def __init__(self, problem: Problem | None = None, *, files: dict | None = None,
                  precision: str = "fp64", device: int = 0, use_graph: bool = True,
-                 verbose: bool = False, grid=None):
+                 verbose: bool = False, grid=None, order: str = "fast"):
         L = N.lib()
         o = N.Opts()
         L.plsqr_default_opts(C.byref(o))
@@ -39,6 +39,9 @@ class Context:
         o.precision = N.PREC_MIXED if precision == "mixed" else N.PREC_FP64
         o.use_graph = int(use_graph)
         o.verbose = int(verbose)
+        if order not in ("fast", "reference"):
+            raise ValueError("order must be 'fast' or 'reference'")
+        o.order = N.ORDER_REFERENCE if order == "reference" else N.ORDER_FAST
         if grid is None and problem is not None:
             grid = problem.meta.get("grid")
         if grid is not None:
@@ -130,6 +133,19 @@ class Context:
                 raise ValueError(f"{nm} must be a contiguous float64 array of {n} values")
         self._check(N.lib().plsqr_aprod_host(self._h, mode, N.ptr(y_k), N.ptr(y_d), N.ptr(x),
                                              iteration, is_final), "plsqr_aprod_host")
+
+    # -- timing report (the reference's GPTL timer names) --------------------
+    def set_timing(self, on: bool = True) -> None:
+        """Time the following FP64 solves per region of every iteration
+        (no CUDA graph while on); see write_timing."""
+        self._check(N.lib().plsqr_set_timing(self._h, int(on)), "plsqr_set_timing")
+
+    def write_timing(self, path: str) -> dict:
+        """Write the last timed solve's JSON report and return it parsed."""
+        import json
+        self._check(N.lib().plsqr_write_timing(self._h, str(path).encode()), "plsqr_write_timing")
+        with open(path) as f:
+            return json.load(f)
 
     # -- driver -------------------------------------------------------------
     def set_reference_x(self, x_ref) -> None:

@@ -115,6 +115,23 @@ class Problem:
         return self.k_csc.num_col
 
 
+def damping_from_params(p: N.SynthParams) -> tuple[Lines, Lines]:
+    """The damping matrix of the parameters, by row and by column (the
+    rows of every column in ascending order, as damping_binary.py's sorted
+    column file holds them)."""
+    L = N.lib()
+    m_d, nnz_d = N.i64(0), N.i64(0)
+    N.check(L.plsqr_synth_damping_size(C.byref(p), C.byref(m_d), C.byref(nnz_d)), "damping_size")
+    drp = np.empty(m_d.value + 1, np.int64)
+    dci = np.empty(nnz_d.value, np.int32)
+    dv = np.empty(nnz_d.value, np.float64)
+    N.check(L.plsqr_synth_damping_fill(C.byref(p), N.ptr(drp), N.ptr(dci), N.ptr(dv)),
+            "damping_fill")
+    n = p.nx * p.ny * p.nz * max(1, p.n_params)
+    d_csr = Lines(drp, dci, dv, int(m_d.value), n)
+    return d_csr, d_csr.transposed(by_col=False)
+
+
 def generate(name_or_dict="grid32", keep_rows: bool = False, **over) -> Problem:
     """Build a synthetic problem.  keep_rows also returns the kernel by row
     (meta['k_csr']); otherwise it is dropped after the transpose."""
@@ -138,17 +155,9 @@ def generate(name_or_dict="grid32", keep_rows: bool = False, **over) -> Problem:
     N.check(L.plsqr_synth_rhs(C.byref(p), N.ptr(rp), N.ptr(ci), N.ptr(kv), N.ptr(x_true),
                               N.ptr(b)), "synth_rhs")
     k_csc = k_csr.transposed(by_col=False)
-    m_d, nnz_d = N.i64(0), N.i64(0)
-    N.check(L.plsqr_synth_damping_size(C.byref(p), C.byref(m_d), C.byref(nnz_d)), "damping_size")
-    drp = np.empty(m_d.value + 1, np.int64)
-    dci = np.empty(nnz_d.value, np.int32)
-    dv = np.empty(nnz_d.value, np.float64)
-    N.check(L.plsqr_synth_damping_fill(C.byref(p), N.ptr(drp), N.ptr(dci), N.ptr(dv)),
-            "damping_fill")
-    d_csr = Lines(drp, dci, dv, int(m_d.value), n)
-    d_csc = d_csr.transposed(by_col=False)
+    d_csr, d_csc = damping_from_params(p)
     meta = dict(grid=(p.nx, p.ny, p.nz), n_rays=m_k, tube_radius=p.tube_radius,
-                nnz_k=nnz, nnz_d=int(nnz_d.value), seed=int(p.seed))
+                nnz_k=nnz, nnz_d=d_csr.nnz, seed=int(p.seed))
     if keep_rows:
         meta["k_csr"] = k_csr
     else:

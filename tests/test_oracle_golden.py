@@ -65,3 +65,43 @@ def test_oracle_thread_count_does_not_change_bits(pkg, orc):
             assert np.array_equal(out["x"], g["x"])
     finally:
         orc.set_threads(n0)
+
+
+def test_oracle_loop_with_operator_callback_is_bitwise_equal(pkg, orc):
+    """The operator-callback form of the oracle's lsqr() (the reference loop
+    driving another aprod) with the oracle's own operator behind the
+    callback gives the reference's bits, and calls it as lsqr.c does."""
+    g = golden("tiny")
+    prob = pkg.read_files(_files("tiny")[1])
+    it = g["meta"]["iterations"]
+    o = orc.OracleProblem(prob)
+    calls = []
+
+    def op(mode, m, n, is_final, iteration):
+        assert (m, n) == (prob.m_k + prob.m_d, prob.n)
+        calls.append((mode, iteration, is_final))
+        o.aprod(mode)
+        return 0
+
+    out = o.lsqr(it, op=op)
+    assert np.array_equal(out["x"], g["x"])
+    assert np.array_equal(out["hist"]["alpha"], g["alpha"])
+    assert np.array_equal(out["hist"]["beta"], g["beta"])
+    assert calls[0] == (2, 0, 0) and len(calls) == 1 + 2 * it
+    assert calls[1:3] == [(1, 1, 0), (2, 1, 0)] and calls[-2:] == [(1, it, 1), (2, it, 1)]
+
+
+def test_oracle_loop_stops_on_operator_error(pkg, orc):
+    prob = pkg.generate("tiny")
+    o = orc.OracleProblem(prob)
+
+    def op(mode, m, n, is_final, iteration):
+        if iteration == 3:
+            raise ValueError("operator failed")
+        o.aprod(mode)
+        return 0
+
+    with pytest.raises(ValueError, match="operator failed"):
+        o.lsqr(10, op=op)
+    with pytest.raises(RuntimeError, match="oracle_lsqr failed"):
+        o.lsqr(10, op=lambda *a: 7)

@@ -1,15 +1,17 @@
 """The product entry point that allocates no device memory.
 
-Callers that run inside CUDA stream capture, or whose device memory belongs to
-another allocator or a fixed budget, cannot let the library call cudaMalloc;
-plsqr_aprod1_nrm2_noalloc takes all of its buffers from the caller and keeps
-its only scratch (one partial sum per block) in a static device array of the
-library.  This file is collected last so that a failure here stops a -x run
-only after every other test has run; it passes alone and after the others.
+Callers whose device memory belongs to another allocator or a fixed budget,
+or that cannot block on the driver's allocator, cannot let the library call
+cudaMalloc; plsqr_aprod1_nrm2_noalloc takes all of its buffers from the caller
+and keeps its only scratch (one partial sum per block) in a static device
+array of the library.  This file is collected last so that a failure here
+stops a -x run only after every other test has run; it passes alone and
+after the others.
 
 Checked through the C ABI against the existing entry point (plsqr_aprod_host
 on a context of the same matrix) with the product tolerance of the parity
-tests, on two calls in a row, plus the size limit."""
+tests, on two calls in a row, plus the size limit, an empty matrix and the
+refusal of unaligned indices or values."""
 from __future__ import annotations
 
 import ctypes as C
@@ -65,3 +67,26 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(pkg):
                                            C.c_void_p(16), C.c_void_p(16), C.c_void_p(16),
                                            C.c_void_p(16), None)
     assert rc == -1  # PLSQR_ERR_ARG, before any device work
+
+
+def test_noalloc_empty_and_misaligned(pkg):
+    """n_rows = 0 writes ||y|| = 0; indices or values that are not 16-byte
+    aligned (the product's vector loads) are refused."""
+    torch = pytest.importorskip("torch")
+    N = pkg._native
+    ptr = torch.zeros(1, dtype=torch.int64, device="cuda")
+    nrm = torch.full((1,), 7.0, dtype=torch.float64, device="cuda")
+    buf = torch.zeros(8, dtype=torch.float64, device="cuda")
+    idx = torch.zeros(8, dtype=torch.int32, device="cuda")
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = N.lib().plsqr_aprod1_nrm2_noalloc(0, C.c_void_p(ptr.data_ptr()), None, None, None,
+                                           None, C.c_void_p(nrm.data_ptr()), s)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert float(nrm.cpu()[0]) == 0.0
+    for i_off, v_off in ((0, 8), (4, 0)):
+        rc = N.lib().plsqr_aprod1_nrm2_noalloc(
+            1, C.c_void_p(ptr.data_ptr()), C.c_void_p(idx.data_ptr() + i_off),
+            C.c_void_p(buf.data_ptr() + v_off), C.c_void_p(buf.data_ptr()),
+            C.c_void_p(buf.data_ptr()), C.c_void_p(nrm.data_ptr()), s)
+        assert rc == -1  # PLSQR_ERR_ARG
