@@ -12,9 +12,13 @@ resident in HBM.
            b_k in and host x out (H2D and D2H inside the timed region)
 
 Extra keys: roofline of the dominant kernel (mode-2 product), the CPU
-baseline (the oracle port, FP64, all host threads, bounded sample), the
-time to 1e-6 relative error vs the FP64 solution for plain FP64 and mixed
-precision, clocks sampled during the timed region.
+baseline (the oracle port, FP64, all host threads, the iteration loop of a
+bounded sample, CPU model), the time to 1e-6 relative error vs the FP64
+solution for plain FP64 and mixed precision (one sweep; the configuration's
+50 iterations per sweep; FP32 vectors as well), the learned warm start +
+mixed precision against both on held-out instances (network trained in the
+run on a bounded set of pairs, --warm-train), clocks sampled during the
+timed region.
 
 `--impl reference` times the reference CPU implementation of the same solve
 (the oracle port of source/lsqr.c + aprod_impl.c + CPUSpMV.c, OpenMP on all
@@ -205,6 +209,11 @@ def main() -> int:
                     help="LSQR iterations of each CPU baseline sample (loop timed alone)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tts", action="store_true", help="skip the time-to-1e-6 runs")
+    ap.add_argument("--warm-train", type=int, default=64,
+                    help="default run: training pairs of the warm-start network (0: skip)")
+    ap.add_argument("--warm-epochs", type=int, default=6)
+    ap.add_argument("--warm-eval", type=int, default=2,
+                    help="default run: held-out instances timed to 1e-6 in the three forms")
     ap.add_argument("--profile", action="store_true",
                     help="profiling run: build the context, run one short solve, exit")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
@@ -358,6 +367,9 @@ def main() -> int:
     extra = {}
     if not args.no_tts and rank == 0:
         extra["time_to_1e-6"] = time_to_tol(pkg, prob, ctx, iters, 1e-6)
+        if args.warm_train > 0:
+            extra["warm_start"] = warm_time_to_tol(pkg, prob, ctx, iters, 1e-6, args.warm_train,
+                                                   args.warm_epochs, args.warm_eval, local)
     ctx.close()
 
     cpu = None
@@ -440,6 +452,122 @@ def time_to_tol(pkg, prob, ctx64, iters, tol) -> dict:
                 out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds"] / min(t)
         else:
             out["mixed"] = {"sweeps": None, "final_err": float(hm["err"][-1])}
+        # the configuration's literal form: 50 inner iterations per sweep, up
+        # to 6 sweeps; reported whether or not it reaches the tolerance
+        cm.set_reference_x(xstar)
+        hl = cm.lsqr(sweeps=6, inner=50)["hist"]
+        cm.set_reference_x(None)
+        kl = first_below(hl["err"], tol)
+        lit = {"sweeps": 6, "inner": 50, "final_err": float(hl["err"][-1]),
+               "inner_iterations_to_tol": kl,
+               "seconds_6_sweeps": min(cm.lsqr(sweeps=6, inner=50)["result"]["seconds_total"]
+                                       for _ in range(2))}
+        if kl is not None:
+            sw = (kl - 1) // 50 + 1
+            lit["sweeps_to_tol"] = sw
+            lit["seconds"] = min(cm.lsqr(sweeps=sw, inner=50)["result"]["seconds_total"]
+                                 for _ in range(2))
+        out["mixed_50_per_sweep"] = lit
+        if "seconds" in out.get("mixed", {}):
+            ms = cm.bench_iteration(reps=20)
+            out["mixed"]["ms_per_inner_iteration"] = ms
+    # FP32 vectors in the inner sweeps as well (PLSQR_MIXED_F32VEC=1)
+    os.environ["PLSQR_MIXED_F32VEC"] = "1"
+    try:
+        with pkg.Context(prob, precision="mixed") as cf:
+            cf.set_reference_x(xstar)
+            hf = cf.lsqr(sweeps=2, inner=inner)["hist"]
+            cf.set_reference_x(None)
+            k = first_below(hf["err"], tol)
+            row = {"form": "FP32 products and FP32 vectors in the inner sweeps; FP64 norms, "
+                           "recurrence and residual refinement", "final_err": float(hf["err"][-1]),
+                   "inner_iterations_to_tol": k, "ms_per_inner_iteration": cf.bench_iteration(reps=20)}
+            if k is not None:
+                sweeps = (k - 1) // inner + 1
+                run = dict(sweeps=1, inner=k) if sweeps == 1 else dict(sweeps=sweeps, inner=inner)
+                row["seconds"] = min(cf.lsqr(**run)["result"]["seconds_total"] for _ in range(3))
+                row.update(run)
+            out["mixed_f32_vectors"] = row
+    finally:
+        os.environ.pop("PLSQR_MIXED_F32VEC", None)
+    out["fp64"]["ms_per_iteration"] = ctx64.bench_iteration(reps=20)
+    return out
+
+
+def warm_time_to_tol(pkg, prob, ctx64, iters, tol, n_train, epochs, n_eval, device) -> dict:
+    """The spec form: learned warm start + mixed precision, against
+    plain FP64 LSQR and cold mixed precision, time to `tol` relative error vs
+    each instance's FP64 solution (FP64 LSQR run to twice the iterations).
+
+    A bounded version of `--extension warm`: the U-Net is trained here on
+    n_train (A^T b, x_LSQR) pairs of the model class (the batched mixed solver
+    makes x_LSQR), for `epochs` passes, and evaluated on n_eval held-out
+    instances of the same class.  The warm time includes the back-projection
+    and the network."""
+    W = pkg.warm
+    grid = prob.meta["grid"]
+    t0 = time.perf_counter()
+    cn2 = W.column_norms2(prob)
+
+    def instance(seed):
+        x_true, b = W.measurements(ctx64, "grid96", grid, seed)
+        return b, W.back_projection(ctx64, b, cn2).astype(np.float32)
+
+    tr = [instance(s) for s in range(n_train)]
+    x_tr, _, _ = W.solve_batches(ctx64, [b for b, _ in tr], iters)
+    t_data = time.perf_counter() - t0
+    rms = lambda v: float(np.sqrt(np.mean(np.asarray(v, np.float64) ** 2)))
+    c = float(np.median([rms(x) / max(rms(z), 1e-300) for x, (_, z) in zip(x_tr, tr)]))
+    t0 = time.perf_counter()
+    net = W.UNet(grid, seed=1, device=device)
+    total, step = epochs * n_train, 0
+    for ep in range(epochs):
+        for i in np.random.default_rng(ep).permutation(n_train):
+            lr = 1e-5 + 0.5 * (1e-3 - 1e-5) * (1.0 + np.cos(np.pi * step / total))
+            net.train_step(tr[i][1], (x_tr[i] / c).astype(np.float32), lr)
+            step += 1
+    t_train = time.perf_counter() - t0
+    rows = []
+    with pkg.Context(prob, precision="mixed", device=device) as cm:
+        for j in range(n_eval):
+            b, z = instance(1_000_000 + j)
+            xs = ctx64.lsqr(b, lsqr_iteration=2 * iters)["x"]
+            ctx64.set_reference_x(xs)
+            k64 = first_below(ctx64.lsqr(b, lsqr_iteration=2 * iters)["hist"]["err"], tol)
+            ctx64.set_reference_x(None)
+            cm.set_reference_x(xs)
+            kc = first_below(cm.lsqr(b, sweeps=1, inner=2 * iters)["hist"]["err"], tol)
+            tp = time.perf_counter()
+            x0 = c * net.predict(W.back_projection(ctx64, b, cn2))
+            t_pre = time.perf_counter() - tp
+            hw = cm.lsqr(b, sweeps=1, inner=2 * iters, x0=x0)
+            kw = first_below(hw["hist"]["err"], tol)
+            cm.set_reference_x(None)
+            row = {"x0_rel_err": float(np.linalg.norm(x0 - xs) / np.linalg.norm(xs)),
+                   "kept_x0": int(hw["result"]["warm"])}
+            if k64 is not None:
+                row["fp64"] = {"iterations": k64, "seconds": min(
+                    ctx64.lsqr(b, lsqr_iteration=k64)["result"]["seconds_total"] for _ in range(2))}
+            if kc is not None:
+                row["mixed"] = {"iterations": kc, "seconds": min(
+                    cm.lsqr(b, sweeps=1, inner=kc)["result"]["seconds_total"] for _ in range(2))}
+            if kw is not None:
+                row["warm_mixed"] = {"iterations": kw, "x0_seconds": t_pre, "seconds": t_pre + min(
+                    cm.lsqr(b, sweeps=1, inner=kw, x0=x0)["result"]["seconds_total"]
+                    for _ in range(2))}
+            rows.append(row)
+    net.close()
+    out = {"tol": tol, "train_pairs": n_train, "epochs": epochs, "heldout_instances": n_eval,
+           "data_seconds": t_data, "train_seconds": t_train, "instances": rows,
+           "model_class": "16-128 Gaussian blobs + checkerboard of period 4-16, 1% noise, "
+                          "measured through the benchmark's kernel matrix",
+           "target": "warm start + mixed precision >= 3x faster than plain FP64"}
+    ok = [r for r in rows if all(k in r for k in ("fp64", "mixed", "warm_mixed"))]
+    if ok:
+        t = {k: float(np.mean([r[k]["seconds"] for r in ok])) for k in ("fp64", "mixed", "warm_mixed")}
+        out["mean_seconds"] = t
+        out["speedup_mixed_vs_fp64"] = t["fp64"] / t["mixed"]
+        out["speedup_warm_mixed_vs_fp64"] = t["fp64"] / t["warm_mixed"]
     return out
 
 

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PLSQR_GPU_ABI_VERSION 1
+#define PLSQR_GPU_ABI_VERSION 2
 
 /* ---- error codes ------------------------------------------------------- */
 #define PLSQR_OK 0
@@ -85,6 +85,14 @@ typedef struct {
   const char *damp_i_bycol; /* -damp_i_bycol int32 nnz per column           */
   const char *b_k;          /* -b_k    ASCII measurement vector             */
   int32_t row_k, row_d, col;
+  /* -col_perm: NULL, or an ASCII file of `col` 1-based column numbers; the
+   * kernel matrix is then loaded with its column i taken from file column
+   * perm[i], as the reference's COL_PERM build does (read_col_perm and
+   * mpiio_load_kernelColBin2ReorderedCSC, source/plsqr3.c:261-283, 1348-1361,
+   * 1652-1713); the damping files and b_k are read as given and x comes out
+   * in the permuted column order (the float64 result file of
+   * source/lsqr.c:95-99 is written so).                                      */
+  const char *col_perm;
 } plsqr_files;
 
 typedef struct {
@@ -444,6 +452,15 @@ int plsqr_io_read_damping(const char *bin_path, int by_col, int32_t m_d,
                           double *val);
 /* b_k, ASCII %le one per line (plsqr3.c:580-589). */
 int plsqr_io_read_rhs(const char *path, int32_t m_k, double *b_k);
+/* read_col_perm (plsqr3.c:1348-1361): n 1-based column numbers, returned
+ * 0-based; PLSQR_ERR_FORMAT when fewer than n or one out of 1..n. */
+int plsqr_io_read_col_perm(const char *path, int32_t n, int32_t *perm);
+/* Column i of the result = column perm[i] of the by-column matrix (ptr, idx,
+ * val over n columns), each column's entries in stored order
+ * (plsqr3.c:1695-1713); tptr holds n + 1 values, tidx / tval the nonzeros of
+ * the selected columns. */
+int plsqr_permute_columns(int32_t n, const int64_t *ptr, const int32_t *idx, const double *val,
+                          const int32_t *perm, int64_t *tptr, int32_t *tidx, double *tval);
 /* Writers of the same formats (the PLSQR3_tools outputs:
  * Ker2PLSQR3.c:499-608, damping_binary.py:75-616). */
 int plsqr_io_write_kernel(const char *bin_path, const char *info_path,

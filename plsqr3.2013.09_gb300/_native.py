@@ -37,7 +37,7 @@ class Files(C.Structure):
     _fields_ = [("dir", C.c_char_p), ("ker_f", C.c_char_p), ("ker_i", C.c_char_p),
                 ("damp_f", C.c_char_p), ("damp_i", C.c_char_p), ("damp_f_bycol", C.c_char_p),
                 ("damp_i_bycol", C.c_char_p), ("b_k", C.c_char_p), ("row_k", i32),
-                ("row_d", i32), ("col", i32)]
+                ("row_d", i32), ("col", i32), ("col_perm", C.c_char_p)]
 
 
 class Opts(C.Structure):
@@ -158,6 +158,8 @@ SIGNATURES = {
     "plsqr_io_read_int32_counts": (C.c_int, [C.c_char_p, i64, vp, C.POINTER(i64)]),
     "plsqr_io_read_damping": (C.c_int, [C.c_char_p, C.c_int, i32, i32, i64, vp, vp, vp]),
     "plsqr_io_read_rhs": (C.c_int, [C.c_char_p, i32, vp]),
+    "plsqr_io_read_col_perm": (C.c_int, [C.c_char_p, i32, vp]),
+    "plsqr_permute_columns": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "plsqr_io_write_kernel": (C.c_int, [C.c_char_p, C.c_char_p, i32, i32, vp, vp, vp]),
     "plsqr_io_write_damping": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, i32,
                                          i32, vp, vp, vp, vp, vp, vp]),

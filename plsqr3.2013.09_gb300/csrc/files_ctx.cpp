@@ -1,6 +1,7 @@
 // plsqr_ctx_create_files: the loading half of PLSQR3_main
-// (source/plsqr3.c:197-589) on one partition: kernel info and records, damping
-// row info and records, damping column info and records, b_k; then the device
+// (source/plsqr3.c:197-589) on one partition: kernel info and records (with
+// the optional column permutation of the COL_PERM build), damping row info
+// and records, damping column info and records, b_k; then the device
 // context.
 #include <stdio.h>
 #include <string.h>
@@ -41,6 +42,22 @@ extern "C" int plsqr_ctx_create_files(const plsqr_files *f, const plsqr_opts *op
     return rc;
   cnt.clear();
   start.clear();
+  if (f->col_perm) {  // COL_PERM (plsqr3.c:261-283, 1652-1713): column i = file column perm[i]
+    std::vector<int32_t> perm((size_t)n);
+    const std::string pf = join(f->dir, f->col_perm);
+    if ((rc = plsqr_io_read_col_perm(pf.c_str(), n, perm.data()))) return rc;
+    std::vector<int64_t> pcp((size_t)n + 1);
+    for (int32_t i = 0; i < n; ++i) pcp[i + 1] = pcp[i] + (kcp[perm[i] + 1] - kcp[perm[i]]);
+    std::vector<int32_t> pri((size_t)pcp[n]);
+    std::vector<double> pv((size_t)pcp[n]);
+    if ((rc = plsqr_permute_columns(n, kcp.data(), kri.data(), kv.data(), perm.data(), pcp.data(),
+                                    pri.data(), pv.data())))
+      return rc;
+    kcp.swap(pcp);
+    kri.swap(pri);
+    kv.swap(pv);
+    nnz_k = kcp[n];
+  }
   // damping by row (plsqr3.c:381-447)
   std::vector<int32_t> dcnt((size_t)m_d);
   int64_t nnz_d = 0;

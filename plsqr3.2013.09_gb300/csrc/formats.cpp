@@ -165,6 +165,37 @@ int plsqr_io_read_rhs(const char *path, int32_t m_k, double *b_k) {
   return PLSQR_OK;
 }
 
+int plsqr_io_read_col_perm(const char *path, int32_t n, int32_t *perm) {
+  if (!path || n < 0 || (n > 0 && !perm)) return PLSQR_ERR_ARG;
+  File in(path, "r");
+  if (!in.f) return PLSQR_ERR_IO;
+  for (int32_t i = 0; i < n; ++i) {
+    int c = 0;
+    if (fscanf(in.f, "%d", &c) != 1 || c < 1 || c > n) return PLSQR_ERR_FORMAT;
+    perm[i] = c - 1;  // 0-based (plsqr3.c:1357)
+  }
+  return PLSQR_OK;
+}
+
+int plsqr_permute_columns(int32_t n, const int64_t *ptr, const int32_t *idx, const double *val,
+                          const int32_t *perm, int64_t *tptr, int32_t *tidx, double *tval) {
+  if (n < 0 || !ptr || !perm || !tptr) return PLSQR_ERR_ARG;
+  tptr[0] = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    if (perm[i] < 0 || perm[i] >= n) return PLSQR_ERR_ARG;
+    tptr[i + 1] = tptr[i] + (ptr[perm[i] + 1] - ptr[perm[i]]);
+  }
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int32_t i = 0; i < n; ++i) {
+    const int64_t a = ptr[perm[i]], k = ptr[perm[i] + 1] - a;
+    if (k > 0) {
+      memcpy(tidx + tptr[i], idx + a, sizeof(int32_t) * (size_t)k);
+      memcpy(tval + tptr[i], val + a, sizeof(double) * (size_t)k);
+    }
+  }
+  return PLSQR_OK;
+}
+
 int plsqr_io_write_kernel(const char *bin_path, const char *info_path, int32_t m_k, int32_t n,
                           const int64_t *col_ptr, const int32_t *row_idx, const double *val) {
   if (!bin_path || !info_path || m_k < 0 || n < 0 || !col_ptr) return PLSQR_ERR_ARG;

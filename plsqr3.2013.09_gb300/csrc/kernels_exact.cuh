@@ -150,12 +150,22 @@ __device__ __forceinline__ double nrm_chain(const NrmArgs &a, const NrmSeg &s) {
   int64_t i0 = 0;
   for (; i0 + 8 <= s.n; i0 += 8) {
     double t[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) t[k] = s.terms[i0 + k];
+    unsigned neg = 0;  // any new scale among the eight (rare: records of a running maximum)
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      if (signbit(t[k])) ssq = dadd(1.0, dmul(dmul(ssq, -t[k]), -t[k]));
-      else ssq = dadd(ssq, t[k]);
+      t[k] = s.terms[i0 + k];
+      neg |= (unsigned)(__double2hiint(t[k]) >> 31);
+    }
+    // the common case keeps one addition per term on the chain (a select
+    // between the two updates would put both multiplies on it as well)
+    if (!neg) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) ssq = dadd(ssq, t[k]);
+    } else {
+      for (int k = 0; k < 8; ++k) {
+        if (signbit(t[k])) ssq = dadd(1.0, dmul(dmul(ssq, -t[k]), -t[k]));
+        else ssq = dadd(ssq, t[k]);
+      }
     }
   }
   for (; i0 < s.n; ++i0) {

@@ -6,8 +6,10 @@
  *              -damp_i_bycol F -b_k F -row_k M -row_d M -col N -itn K
  * and the same outputs as call_lsqr (source/lsqr.c:34-184): result.txt in the
  * working directory and the float64 solution
- * p_resultx_itn=<K>_NProc=1_float64_mpiio.bin.  -row_ptn, -col_ptn and
- * -col_perm describe a multi-rank partition and are accepted and ignored.
+ * p_resultx_itn=<K>_NProc=1_float64_mpiio.bin.  -row_ptn and -col_ptn
+ * describe a multi-rank partition and are accepted and ignored; -col_perm
+ * FILE loads the kernel with its columns permuted, as the reference's
+ * COL_PERM build does (the solution then comes out in the permuted order).
  * Additional options: -precision fp64|mixed, -sweeps S, -inner I, -device G,
  * -quiet, -x0 FILE: a starting solution for the mixed solver, col raw
  * float64 values (the format of the solution file above), kept where it
@@ -31,7 +33,7 @@ int main(int argc, char **argv) {
   const char *damp_i_c = "plsqr3_reorder_small_all.damp.bycol.info.bin";
   const char *damp_f_c = "plsqr3_reorder_small_all.damp.bycol.bin";
   const char *b_k = "vecotrB_ker";
-  const char *x0_path = NULL, *timing_path = NULL;
+  const char *x0_path = NULL, *timing_path = NULL, *col_perm = NULL;
   int order = PLSQR_ORDER_FAST;
   int row_k = 10, row_d = 1825, col = 520, itn = 40;
   int precision = PLSQR_PREC_FP64, sweeps = 4, inner = 50, device = 0, verbose = 1;
@@ -67,7 +69,8 @@ int main(int argc, char **argv) {
     INT("-sweeps", sweeps);
     INT("-inner", inner);
     INT("-device", device);
-    if ((!strcmp(a, "-row_ptn") || !strcmp(a, "-col_ptn") || !strcmp(a, "-col_perm")) && v) {
+    STR("-col_perm", col_perm);
+    if ((!strcmp(a, "-row_ptn") || !strcmp(a, "-col_ptn")) && v) {
       fprintf(stderr, "%s ignored: one GPU holds the whole problem\n", a);
       i++;
       continue;
@@ -101,6 +104,7 @@ int main(int argc, char **argv) {
   f.row_k = row_k;
   f.row_d = row_d;
   f.col = col;
+  f.col_perm = col_perm;
   plsqr_opts o;
   plsqr_default_opts(&o);
   o.device = device;

@@ -54,6 +54,7 @@ class Context:
                 setattr(f, k, str(files[k]).encode())
             f.dir = str(files["dir"]).encode()
             f.row_k, f.row_d, f.col = int(files["row_k"]), int(files["row_d"]), int(files["col"])
+            f.col_perm = str(files["col_perm"]).encode() if files.get("col_perm") else None
             N.check(L.plsqr_ctx_create_files(C.byref(f), C.byref(o), C.byref(h)),
                     "plsqr_ctx_create_files")
         else:

@@ -91,6 +91,29 @@ class Lines:
         return Lines(tptr, tidx, tval, self.num_row, self.num_col)
 
 
+def permute_columns(k_csc: Lines, perm) -> Lines:
+    """The by-column matrix with column i taken from column perm[i] (the
+    COL_PERM loader, source/plsqr3.c:1695-1713)."""
+    perm = np.ascontiguousarray(perm, np.int32)
+    n = k_csc.num_col
+    if perm.shape != (n,):
+        raise ValueError(f"perm must hold {n} column numbers")
+    cnt = k_csc.ptr[perm.astype(np.int64) + 1] - k_csc.ptr[perm]
+    tptr = np.zeros(n + 1, np.int64)
+    np.cumsum(cnt, out=tptr[1:])
+    tidx = np.empty(int(tptr[-1]), np.int32)
+    tval = np.empty(int(tptr[-1]), np.float64)
+    N.check(N.lib().plsqr_permute_columns(n, N.ptr(k_csc.ptr), N.ptr(k_csc.idx),
+                                          N.ptr(k_csc.val), N.ptr(perm), N.ptr(tptr),
+                                          N.ptr(tidx), N.ptr(tval)), "plsqr_permute_columns")
+    return Lines(tptr, tidx, tval, k_csc.num_row, n)
+
+
+def write_col_perm(path, perm) -> None:
+    """A column permutation file: one 1-based column number per line."""
+    Path(path).write_text("".join(f"{int(c) + 1}\n" for c in perm))
+
+
 @dataclass
 class Problem:
     """The operator in the reference's in-memory layout plus b_k and x_true."""

@@ -30,7 +30,7 @@ tests/golden/socal25 comes from the reference's own data/ sample (its first
 25 rays; see run_socal).
 
 Usage: python tests/golden/make_golden.py [case ...]   (default: tiny grid32)
-       cases: tiny grid32 grid96s grid96 socal25
+       cases: tiny grid32 grid96s grid96 socal25 grid32p
        python tests/golden/make_golden.py --ulp case ...  (ulp.txt only)
 The 200,000-ray case writes 21 GB of input files to the temporary directory
 and takes about an hour on 8 cores (the reference's kernel-row product is
@@ -284,6 +284,60 @@ def run_socal(pkg, orc, ref: Path, n_rays: int = SOCAL_RAYS) -> None:
           flush=True)
 
 
+# ---- the column permutation of the COL_PERM build ------------------------------
+PERM_SEED = 2013
+
+
+def run_col_perm(pkg, orc, ref: Path, base: str = "grid32") -> None:
+    """tests/golden/<base>p: the reference's solve of <base> with its kernel
+    columns permuted as the COL_PERM build loads them (column i = file column
+    perm[i], damping and b as given, x in the permuted order).  That build
+    itself cannot run: source/plsqr3.c:283 frees the column info array and
+    sets it to NULL, and :328-329 hand the NULL to the reordered loader,
+    which dereferences it (:1698).  Its loader is a pure selection of
+    columns, so the reference program is run on the kernel file written with
+    the columns already permuted: the matrix that loader would build.  The
+    permutation is numpy's PCG64 permutation of seed PERM_SEED."""
+    name = base + "p"
+    out = HERE / name
+    it = pkg.CONFIGS[base]["iterations"]
+    prob = pkg.generate(base)
+    perm = np.random.default_rng(PERM_SEED).permutation(prob.n).astype(np.int32)
+    kp = pkg.synth.permute_columns(prob.k_csc, perm)
+    permuted = pkg.Problem(kp, prob.d_csr, prob.d_csc, prob.b_k, prob.x_true, it, prob.meta)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        files = pkg.write_files(permuted, td / "in")
+        pkg.synth.write_col_perm(td / "colPerm", perm)
+        run = td / "run"
+        run.mkdir()
+        cmd = [str(ref), "-dir", str(td / "in")]
+        for k in INPUT_KEYS:
+            cmd += [f"-{k}", files[k]]
+        cmd += ["-row_k", str(prob.m_k), "-row_d", str(prob.m_d), "-col", str(prob.n),
+                "-itn", str(it)]
+        r = subprocess.run(cmd, cwd=run, capture_output=True, text=True, check=True)
+        lines = r.stdout.splitlines()
+        al = [l.split()[1] for l in lines if l.startswith("ORACLE_alpha")]
+        be = [l.split()[1] for l in lines if l.startswith("ORACLE_beta")]
+        assert len(al) == len(be) == it + 1
+        if out.exists():
+            shutil.rmtree(out)
+        out.mkdir()
+        shutil.copy(run / f"p_resultx_itn={it}_NProc=1_float64_mpiio.bin", out / "x.f64")
+        shutil.copy(run / "result.txt", out / "result.txt")
+        (out / "alpha_beta.txt").write_text(
+            "".join(f"{k} {a} {b}\n" for k, (a, b) in enumerate(zip(al, be))))
+        meta = dict(case=name, base=base, iterations=it, perm_seed=PERM_SEED,
+                    col_perm_sha256=sha256(td / "colPerm"),
+                    permuted_kernel_sha256={files[k]: sha256(td / "in" / files[k])
+                                            for k in ("ker_f", "ker_i")},
+                    files={k: v for k, v in files.items() if k != "dir"} | {"dir": "inputs"},
+                    reference_time=[l for l in lines if "Parallel LSQR time" in l])
+        (out / "meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
+    print(f"{name}: {it} iterations with permuted columns, written to {out}", flush=True)
+
+
 def main(names) -> None:
     pkg = g.load_package()
     orc = g.load_oracle()
@@ -298,6 +352,9 @@ def main(names) -> None:
     for name in names:
         if name.startswith("socal"):
             run_socal(pkg, orc, ref, int(name[5:] or SOCAL_RAYS))
+            continue
+        if name.endswith("p") and name[:-1] in CASES:
+            run_col_perm(pkg, orc, ref, name[:-1])
             continue
         run_case(name, pkg, orc, ref)
         if CASES[name][1]:
