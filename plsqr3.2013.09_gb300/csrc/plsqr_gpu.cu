@@ -25,6 +25,7 @@
 #include "plsqr_internal.h"
 #include "slab.cuh"
 #include "transpose.cuh"
+#include "units.cuh"
 
 using namespace plsqr;
 
@@ -272,10 +273,31 @@ int slab_set_smem(size_t smem) {
 template int slab_set_smem<double>(size_t);
 template int slab_set_smem<float>(size_t);
 
+void units_spmv(const DevUnits &U, const double *x, cudaStream_t s) {
+  const UnitsArgs A{U.idx, U.val, U.slot0, U.q, U.c, U.line, U.unit_begin,
+                    U.n_lines, U.n_slabs, U.slab, U.n_idx};
+  cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
+  k_slab_units<1024><<<U.blocks, 1024, U.smem, s>>>(A, U.next, x, U.partial);
+}
+
+int units_set_smem(size_t smem) {
+  return cudaFuncSetAttribute(k_slab_units<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)std::max<size_t>(smem, 1))
+             ? PLSQR_ERR_CUDA
+             : PLSQR_OK;
+}
+
 static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
   if (ctx->exact) {  // the reference's order (kernels_exact.cuh); no partial sums
     k_ref_rows<kThreads><<<ctx->ex_gk + ctx->ex_gd, kThreads, 0, s>>>(
         ctx->K.csr(), ctx->D.csr(), ctx->v, ctx->u, ctx->ex_gk, mode, ctx->st);
+    return;
+  }
+  if (ctx->use_units_rows) {
+    const DevUnits &U = ctx->u_rows;
+    units_spmv(U, ctx->v, s);
+    k_combine_rows<double, double, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
+        U.partial, U.n_slabs, ctx->m_k, ctx->D.csr(), ctx->v, ctx->u, ctx->gc1k, mode, ctx->st, parts);
     return;
   }
   if (ctx->use_slabs_rows) {
@@ -297,6 +319,13 @@ static void m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
                                                           ctx->m_k, ctx->v, mode, ctx->st);
     return;
   }
+  if (ctx->use_units) {
+    const DevUnits &U = ctx->u_cols;
+    units_spmv(U, ctx->u, s);
+    k_combine_cols<double, double, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+        U.partial, U.n_slabs, ctx->n, ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, mode, ctx->st, parts);
+    return;
+  }
   if (ctx->use_slabs) {
     const DevSlab<double> &S = ctx->s_cols;
     slab_spmv(S, ctx->slab_group, ctx->u, s);
@@ -314,7 +343,9 @@ static void m2(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
 // per-module attribute, so it is set here, where the kernel is launched.
 static int slab_attrs(plsqr_ctx *ctx) {
   if (!ctx->use_slabs && !ctx->use_slabs_rows) return PLSQR_OK;
-  const int rc = slab_set_smem<double>(std::max(ctx->s_rows.smem, ctx->s_cols.smem));
+  int rc = slab_set_smem<double>(std::max(ctx->s_rows.smem, ctx->s_cols.smem));
+  if (!rc && (ctx->use_units || ctx->use_units_rows))
+    rc = units_set_smem(std::max(ctx->u_cols.smem, ctx->u_rows.smem));
   if (rc) ctx_set_error(ctx, "cudaFuncSetAttribute failed for the slab kernels");
   return rc;
 }

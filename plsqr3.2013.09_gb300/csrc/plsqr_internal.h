@@ -39,6 +39,20 @@ struct DevSlab {
   int chunk = 4;  // passes of lines a warp takes per counter grab
 };
 
+// The kernel matrix by column or by row in the unit layout (units.cuh).
+struct DevUnits {
+  uint16_t *idx = nullptr;
+  double *val = nullptr;
+  int64_t *slot0 = nullptr;
+  int32_t *q = nullptr, *c = nullptr, *line = nullptr, *unit_begin = nullptr;
+  int32_t n_lines = 0, n_slabs = 0, slab = 0, n_idx = 0, n_units = 0;
+  int64_t slots = 0;
+  int *next = nullptr;         // [n_slabs] unit counters, zeroed before every launch
+  double *partial = nullptr;   // [n_slabs * n_lines]
+  int blocks = 0;
+  size_t smem = 0;
+};
+
 struct MixedState;  // mixed.cu
 struct BatchState;  // batched.cu
 
@@ -75,6 +89,10 @@ struct plsqr_ctx {
   int slab_group = 8;      // lanes per segment, FP64 slab products
   int slab_group_f = 16;   // lanes per segment, FP32 slab products
   DevSlab<double> s_rows, s_cols;  // K by row (gathers v), K by column (gathers u_k)
+  bool use_units = false;          // FP64 A^T y on the unit layout (default)
+  DevUnits u_cols;                 // K by column in the unit layout
+  bool use_units_rows = false;     // FP64 A x on the unit layout
+  DevUnits u_rows;                 // K by row in the unit layout
   int gc1k = 1, gc1d = 1, gc2 = 1;  // grids of the combine kernels
   BatchState *batch = nullptr;       // several right-hand sides (batched.cu)
   double *d_val0 = nullptr, *dc_val0 = nullptr;  // damping values before weighting
@@ -108,6 +126,10 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, i
 // persistent grid or 0.
 int slab_dyn_blocks(const plsqr_ctx *ctx, bool fp32);
 int slab_plan(plsqr_ctx *ctx);
+int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevUnits *out);
+// plsqr_gpu.cu: unit product launch and its shared-memory attribute
+void units_spmv(const DevUnits &U, const double *x, cudaStream_t s);
+int units_set_smem(size_t smem);
 // plsqr_gpu.cu: slab product launch and its shared-memory attribute
 template <typename T>
 void slab_spmv(const DevSlab<T> &S, int group, const T *x, cudaStream_t s);

@@ -9,6 +9,7 @@
 
 #include "plsqr_internal.h"
 #include "slab.cuh"
+#include "units.cuh"
 
 using namespace plsqr;
 
@@ -130,15 +131,111 @@ template int build_slab<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
 template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, int,
                                DevSlab<float> *, int, int);
 
+// The unit layout (units.cuh) of a by-line matrix: segments counted as for
+// the slab layout, lines of each slab sorted longest segment first and cut
+// into units of kUnitLines, every unit's groups assigned to 32 lanes.
+int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevUnits *out) {
+  const int n_lines = L.n_lines;
+  const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
+  if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
+  int rc;
+  const int64_t cells = (int64_t)n_slabs * n_lines;
+  int64_t *cnt = nullptr;
+  if ((rc = dev_alloc(ctx, &cnt, (size_t)std::max<int64_t>(cells, 1)))) return rc;
+  const int g = std::max(1, std::min(ctx->sm_count * 8, (n_lines + 255) / 256));
+  k_slab_count<<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, n_lines, n_slabs, slab, cnt);
+  CK(cudaGetLastError());
+  std::vector<int64_t> hc((size_t)std::max<int64_t>(cells, 1));
+  CK(cudaMemcpyAsync(hc.data(), cnt, sizeof(int64_t) * cells, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, cnt);
+  // units: per slab, lines longest segment first (ties by line), 32 at a time
+  std::vector<int32_t> ubeg((size_t)n_slabs + 1, 0), uq, uc, uline, seg_unit((size_t)cells),
+      seg_pos((size_t)cells);
+  std::vector<int64_t> uslot;
+  int64_t slots = 0;
+  std::vector<int32_t> ord((size_t)n_lines);
+  for (int s = 0; s < n_slabs; ++s) {
+    const int64_t *cs = hc.data() + (size_t)s * n_lines;
+    for (int l = 0; l < n_lines; ++l) ord[(size_t)l] = l;
+    std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return cs[a] > cs[b]; });
+    ubeg[(size_t)s] = (int32_t)uq.size();
+    for (int i0 = 0; i0 < n_lines; i0 += kUnitLines) {
+      const int u = (int)uq.size();
+      int64_t run = 0;
+      for (int i = 0; i < kUnitLines; ++i) {
+        uc.push_back((int32_t)run);
+        if (i0 + i < n_lines) {
+          const int l = ord[(size_t)i0 + i];
+          uline.push_back(l);
+          seg_unit[(size_t)s * n_lines + l] = u;
+          seg_pos[(size_t)s * n_lines + l] = i;
+          run += cs[l] / 8;
+        } else {
+          uline.push_back(-1);
+        }
+      }
+      uc.push_back((int32_t)run);
+      if (run > INT32_MAX / 2) return PLSQR_ERR_ARG;
+      const int64_t q = (run + 31) / 32;
+      uq.push_back((int32_t)q);
+      uslot.push_back(slots);
+      slots += 32 * q;
+    }
+  }
+  ubeg[(size_t)n_slabs] = (int32_t)uq.size();
+  out->n_lines = n_lines;
+  out->n_slabs = n_slabs;
+  out->slab = slab;
+  out->n_idx = n_idx;
+  out->n_units = (int32_t)uq.size();
+  out->slots = slots;
+  int32_t *d_seg_unit = nullptr, *d_seg_pos = nullptr;
+  if ((rc = dev_alloc(ctx, &out->idx, (size_t)slots * 8)) ||
+      (rc = dev_alloc(ctx, &out->val, (size_t)slots * 8)) ||
+      (rc = dev_alloc(ctx, &out->slot0, uslot.size())) || (rc = dev_alloc(ctx, &out->q, uq.size())) ||
+      (rc = dev_alloc(ctx, &out->c, uc.size())) || (rc = dev_alloc(ctx, &out->line, uline.size())) ||
+      (rc = dev_alloc(ctx, &out->unit_begin, ubeg.size())) ||
+      (rc = dev_alloc(ctx, &out->next, (size_t)n_slabs)) ||
+      (rc = dev_alloc(ctx, &out->partial, (size_t)std::max<int64_t>(cells, 1))) ||
+      (rc = dev_alloc(ctx, &d_seg_unit, seg_unit.size())) ||
+      (rc = dev_alloc(ctx, &d_seg_pos, seg_pos.size())))
+    return rc;
+  CK(cudaMemsetAsync(out->idx, 0, sizeof(uint16_t) * 8 * (size_t)std::max<int64_t>(slots, 1),
+                     ctx->stream));
+  CK(cudaMemsetAsync(out->val, 0, sizeof(double) * 8 * (size_t)std::max<int64_t>(slots, 1),
+                     ctx->stream));
+  CK(cudaMemcpy(out->slot0, uslot.data(), sizeof(int64_t) * uslot.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(out->q, uq.data(), sizeof(int32_t) * uq.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(out->c, uc.data(), sizeof(int32_t) * uc.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(out->line, uline.data(), sizeof(int32_t) * uline.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(out->unit_begin, ubeg.data(), sizeof(int32_t) * ubeg.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_seg_unit, seg_unit.data(), sizeof(int32_t) * seg_unit.size(),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_seg_pos, seg_pos.data(), sizeof(int32_t) * seg_pos.size(), cudaMemcpyHostToDevice));
+  const UnitsArgs U{out->idx, out->val, out->slot0, out->q, out->c, out->line, out->unit_begin,
+                    n_lines, n_slabs, slab, n_idx};
+  k_units_fill<<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, L.val, n_lines, n_slabs, slab, d_seg_unit,
+                                           d_seg_pos, U, out->idx, out->val);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  dev_free(ctx, d_seg_unit);
+  dev_free(ctx, d_seg_pos);
+  out->blocks = ctx->sm_count;
+  out->smem = units_smem((size_t)std::min(slab, n_idx), 1024);
+  return PLSQR_OK;
+}
+
 // Plan the slab paths.  slab_ok: every dimension fits kMaxSlabs slabs of
 // 24,576 FP32 values, so the mixed solver's inner products use FP32 slabs.
-// FP64: A^T y uses slabs of 24,576 values (its gathers of u_k scatter over
-// L2, and shared memory serves them faster); A x keeps the per-line kernel
-// (its gathers of v hit nearby columns and already run near the HBM
-// roofline, while slab segments would add FP64 reductions).  PLSQR_SLABS
-// overrides: 0 none, 1 both orientations, 2 A^T y only (default).
+// FP64: both products on slabs of 24,576 values in the unit layout
+// (units.cuh): on the 96x96x32 problem A^T y 2.66 -> 2.30 ms and A x 2.57 ->
+// 2.31 ms against the segment-per-group slab kernel and the per-row kernel
+// k_aprod1 (16-bit indices, every lane busy, the gathered vector in shared
+// memory).  PLSQR_SLABS overrides: 0 none, 1 both orientations (default),
+// 2 A^T y only; PLSQR_SLAB_UNITS=0 the slab kernel instead of the units.
 int slab_plan(plsqr_ctx *ctx) {
-  ctx->use_slabs = ctx->use_slabs_rows = false;
+  ctx->use_slabs = ctx->use_slabs_rows = ctx->use_units = ctx->use_units_rows = false;
   const int fslab = 24576;
   ctx->slab_ok = ctx->nnz_k > 0 && (ctx->n + fslab - 1) / fslab <= kMaxSlabs &&
                  (ctx->m_k + fslab - 1) / fslab <= kMaxSlabs;
@@ -146,7 +243,7 @@ int slab_plan(plsqr_ctx *ctx) {
   ctx->gc1k = std::max(1, std::min({sm * 2, (ctx->m_k + 255) / 256, half}));
   ctx->gc1d = std::max(1, std::min({sm * 2, (ctx->m_d + 255) / 256, half}));
   ctx->gc2 = std::max(1, std::min({sm * 4, (ctx->n + 255) / 256, kMaxParts}));
-  int mode = 2;
+  int mode = 1;
   if (const char *e = getenv("PLSQR_SLABS")) mode = atoi(e);
   int slab = 24576;  // 192 KB of FP64 per block
   if (const char *s = getenv("PLSQR_SLAB_SIZE"))
@@ -155,16 +252,28 @@ int slab_plan(plsqr_ctx *ctx) {
   const bool cols_fit = (ctx->m_k + slab - 1) / slab <= kMaxSlabs;
   if (ctx->nnz_k == 0 || mode <= 0) return PLSQR_OK;
   int rc;
+  // the unit layout unless PLSQR_SLAB_UNITS=0 (or the slab and its summing
+  // area do not fit in shared memory)
+  int units = 1;
+  if (const char *e = getenv("PLSQR_SLAB_UNITS")) units = atoi(e) != 0;
   if (mode == 1 && rows_fit) {
-    if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &ctx->s_rows, 0,
-                                 slab_dyn_blocks(ctx, false))))
+    if (units && units_smem((size_t)std::min(slab, ctx->n), 1024) <= 227 * 1024) {
+      if ((rc = build_units(ctx, ctx->K, ctx->n, slab, &ctx->u_rows))) return rc;
+      ctx->use_units_rows = true;
+    } else if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &ctx->s_rows,
+                                        0, slab_dyn_blocks(ctx, false)))) {
       return rc;
+    }
     ctx->use_slabs_rows = true;
   }
   if ((mode == 1 || mode == 2) && cols_fit) {
-    if ((rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &ctx->s_cols, 0,
-                                 slab_dyn_blocks(ctx, false))))
+    if (units && units_smem((size_t)std::min(slab, ctx->m_k), 1024) <= 227 * 1024) {
+      if ((rc = build_units(ctx, ctx->KC, ctx->m_k, slab, &ctx->u_cols))) return rc;
+      ctx->use_units = true;
+    } else if ((rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count,
+                                        &ctx->s_cols, 0, slab_dyn_blocks(ctx, false)))) {
       return rc;
+    }
     ctx->use_slabs = true;
   }
   return PLSQR_OK;

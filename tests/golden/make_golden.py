@@ -24,7 +24,7 @@ so that a GPU test can hold every iteration of the big solve against the
 reference without running a CPU solve of its own.
 
 The large cases also get ulp.txt: how far the reference's own scalars move
-under a one-ulp change of b_k[0] (see ulp_sensitivity).
+when every element of b_k is raised by one ulp (see ulp_sensitivity).
 
 tests/golden/socal25 comes from the reference's own data/ sample (its first
 25 rays; see run_socal).
@@ -151,40 +151,44 @@ def run_case(name: str, pkg, orc, ref: Path) -> None:
 
 
 def ulp_sensitivity(name: str, pkg, orc) -> None:
-    """How far the reference's own per-iteration scalars move when b_k[0] is
-    raised by one ulp: the oracle (bitwise equal to the reference) is run on
-    the perturbed b and compared with the stored golden run.  Written to
+    """How far the reference's own per-iteration scalars move when every
+    element of b_k is raised by one ulp (a change of the size of the
+    rounding differences between two summation orders; one element alone is
+    absorbed by the rounding of the first norm and product on the 200,000-ray
+    problem): the oracle (bitwise equal to the reference) is run on the
+    perturbed b and compared with the stored golden run.  Written to
     <case>/ulp.txt (k, then the relative change of alpha, beta, rnorm,
-    arnorm) and meta.json["ulp_x_rel"] (the change of x).  Runs from the
-    committed golden files; the reference tree is not needed."""
+    arnorm) and, while x.f64 is still there (right after the golden run),
+    meta.json["ulp_x_rel"] (the change of x), after which x.f64 is replaced by
+    its digest.  The reference tree is not needed."""
     out = HERE / name
     meta = json.loads((out / "meta.json").read_text())
     it = meta["iterations"]
-    if not (out / "x.f64").exists():
-        raise SystemExit(f"{name}: x.f64 is gone (ulp.txt is made right after the golden run)")
     prob = pkg.generate(name)
     assert array_digest(prob) == meta["array_sha256"]
-    b = prob.b_k.copy()
-    b[0] = np.nextafter(b[0], np.inf)
+    b = np.nextafter(prob.b_k, np.inf)
     t0 = time.time()
     o = orc.OracleProblem(prob).lsqr(it, b_k=b)
     print(f"{name}: perturbed oracle run in {time.time() - t0:.0f} s", flush=True)
     ab = np.loadtxt(out / "alpha_beta.txt")
     hist = np.loadtxt(out / "hist.txt")
-    x = np.fromfile(out / "x.f64", np.float64)
     rel = lambda a, r: np.abs(a - r) / np.maximum(np.abs(r), 1e-300)
     cols = [rel(o["hist"]["alpha"], ab[:, 1]), rel(o["hist"]["beta"], ab[:, 2]),
             rel(o["hist"]["rnorm"], hist[:, 1]), rel(o["hist"]["arnorm"], hist[:, 2])]
     (out / "ulp.txt").write_text(
-        "# relative change of the reference's scalars under a one-ulp raise of b_k[0]\n"
-        "# k alpha beta rnorm arnorm\n"
+        "# relative change of the reference's scalars when every element of b_k is raised "
+        "by one ulp\n# k alpha beta rnorm arnorm\n"
         + "".join(f"{k} " + " ".join(f"{c[k]:.3e}" for c in cols) + "\n" for k in range(it + 1)))
-    meta["ulp_x_rel"] = float(np.linalg.norm(o["x"] - x) / np.linalg.norm(x))
-    # the large cases keep the digest of x, not x (2.4 MB): a GPU test holds
-    # its reference-order x to the digest and its other x to that one
-    meta["x_sha256"] = hashlib.sha256(x.tobytes()).hexdigest()
+    xf = out / "x.f64"
+    meta.pop("ulp_x_rel", None)
+    if xf.exists():
+        x = np.fromfile(xf, np.float64)
+        meta["ulp_x_rel"] = float(np.linalg.norm(o["x"] - x) / np.linalg.norm(x))
+        # the large cases keep the digest of x, not x (2.4 MB): a GPU test
+        # holds its reference-order x to the digest and its other x to that one
+        meta["x_sha256"] = hashlib.sha256(x.tobytes()).hexdigest()
+        xf.unlink()
     (out / "meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
-    (out / "x.f64").unlink()
 
 
 # ---- the reference's data/ sample (SoCal): its first SOCAL_RAYS rays ----------

@@ -20,18 +20,22 @@ def per_iter_rel(a, b):
 
 
 FP64_CASES = [
-    {"PLSQR_SLABS": "0"},                                   # per-line A^T y (k_aprod2)
+    {"PLSQR_SLABS": "0"},                                   # per-line products (k_aprod1/2)
     {"PLSQR_SLABS": "0", "PLSQR_M2_BLOCKS_PER_SM": "3"},
-    {"PLSQR_SLABS": "1"},                                   # FP64 row slabs for A x too
+    {"PLSQR_SLABS": "2"},                                   # k_aprod1 for A x, units for A^T y
     {"PLSQR_SLAB_SIZE": "1024"},                            # many slabs, short segments
-    {"PLSQR_SLABS": "1", "PLSQR_SLAB_SIZE": "1024"},
-    {"PLSQR_SLAB_GROUP": "4"},
-    {"PLSQR_SLAB_GROUP": "16"},
-    {"PLSQR_SLAB_GROUP": "32"},
-    {"PLSQR_SLAB_BLOCKS": "7"},
-    {"PLSQR_UNROLL": "1"},
-    {"PLSQR_UNROLL": "4"},
-    {"PLSQR_BLOCKS_PER_SM": "1"},
+    {"PLSQR_SLAB_SIZE": "28672"},                           # units do not fit: slab kernels
+    {"PLSQR_SLAB_UNITS": "0"},                              # slab kernels, persistent
+    {"PLSQR_SLAB_UNITS": "0", "PLSQR_SLAB_SCHED": "0"},     # slab kernels, static blocks
+    {"PLSQR_SLAB_UNITS": "0", "PLSQR_SLAB_SIZE": "1024"},
+    {"PLSQR_SLAB_UNITS": "0", "PLSQR_SLAB_GROUP": "4"},
+    {"PLSQR_SLAB_UNITS": "0", "PLSQR_SLAB_GROUP": "16"},
+    {"PLSQR_SLAB_UNITS": "0", "PLSQR_SLAB_GROUP": "32"},
+    {"PLSQR_SLAB_UNITS": "0", "PLSQR_SLAB_CHUNK": "1"},
+    {"PLSQR_SLAB_UNITS": "0", "PLSQR_SLAB_SCHED": "0", "PLSQR_SLAB_BLOCKS": "7"},
+    {"PLSQR_SLABS": "2", "PLSQR_UNROLL": "1"},
+    {"PLSQR_SLABS": "2", "PLSQR_UNROLL": "4"},
+    {"PLSQR_SLABS": "2", "PLSQR_BLOCKS_PER_SM": "1"},
     {"PLSQR_NATURAL_ORDER": "1", "PLSQR_SLABS": "0"},
 ]
 
