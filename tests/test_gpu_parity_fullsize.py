@@ -12,7 +12,11 @@ here and checked against the digest of the arrays the reference read.
   kept in meta.json) and every iteration's scalars equal the reference's bit
   for bit, all 300 iterations; result.txt is the same text.
 * the default order (parallel sums): x within 1e-10 of the reference's (of
-  the reference-order x, whose digest is the reference's).
+  the reference-order x, whose digest is the reference's), or within ten
+  times the change of the reference's own x under the one-ulp probe below
+  where that is larger: on the 200,000-ray problem 300 iterations stop short
+  of convergence (1e-6 of the solution takes ~376), and the reference's x
+  there moves by 1.2e-6 when every element of b_k is raised by one ulp.
   Per iteration the bar is 1e-10 over the iterations where the reference's
   own scalars are well conditioned: ulp.txt records how far they move when
   every element of b_k is raised by one ulp (a change of the size of the
@@ -145,14 +149,19 @@ def test_fast_order_matches_reference_fullsize(case, pkg, big, ref_order, tmp_pa
     for k in HIST_KEYS:
         dev[k] = np.concatenate([[0.0], rel_each(h[k][1:], gh[k][1:])])
     ex = rel(out["x"], xr)
+    # the reference's own sensitivity, where the golden run recorded it
+    x_bar = max(LSQR_TOL, 10.0 * g["meta"].get("ulp_x_rel", 0.0))
+    u_last = np.loadtxt(GOLDEN / case / "ulp.txt")[-1]
+    r_bar = max(LSQR_TOL, 10.0 * u_last[3])
     print(f"{case}: default order, x within {ex:.2e} of the reference; per iteration, "
           f"k < {ks}: " + ", ".join(f"{k} {np.max(v[:ks]):.1e}" for k, v in dev.items())
-          + "; all k: " + ", ".join(f"{k} {np.max(v):.1e}" for k, v in dev.items()))
-    assert ex <= LSQR_TOL
+          + "; all k: " + ", ".join(f"{k} {np.max(v):.1e}" for k, v in dev.items())
+          + f"; bars: x {x_bar:.1e}, final rnorm {r_bar:.1e}")
+    assert ex <= x_bar
     assert ks >= 10, "the reference is ill-conditioned from the first iterations"
     for k, v in dev.items():
         assert np.max(v[:ks]) <= LSQR_TOL, (k, int(np.argmax(v[:ks])), float(np.max(v[:ks])))
     # converged quantities at the end of the solve
-    for k in ("rnorm", "xnorm"):
-        assert dev[k][-1] <= LSQR_TOL, k
+    assert dev["rnorm"][-1] <= r_bar
+    assert dev["xnorm"][-1] <= x_bar
     check_result_txt(tmp_path / "result.txt", g)
