@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PLSQR_GPU_ABI_VERSION 2
+#define PLSQR_GPU_ABI_VERSION 3
 
 /* ---- error codes ------------------------------------------------------- */
 #define PLSQR_OK 0
@@ -106,6 +106,13 @@ typedef struct {
    * rays are gathered together.  Zeros: natural column order. */
   int32_t grid[3];
   int32_t order; /* PLSQR_ORDER_* (FP64 contexts; mixed precision needs FAST) */
+  /* Nonzero: once the unit layouts hold both FP64 products, release the
+   * by-row and by-column copies of K they were built from (device memory
+   * about 1.7x the 16 bytes per nonzero instead of 3.7x).  FP64 contexts in
+   * the fast order only (PLSQR_ERR_ARG otherwise).  plsqr_lsqr and
+   * plsqr_aprod are unchanged, bit for bit; the batched solver, which reads
+   * those copies, returns PLSQR_ERR_STATE on such a context. */
+  int32_t lean;
 } plsqr_opts;
 
 typedef struct {

@@ -42,7 +42,7 @@ class Files(C.Structure):
 
 class Opts(C.Structure):
     _fields_ = [("device", i32), ("precision", i32), ("use_graph", i32), ("verbose", i32),
-                ("grid", i32 * 3), ("order", i32)]
+                ("grid", i32 * 3), ("order", i32), ("lean", i32)]
 
 
 class Info(C.Structure):

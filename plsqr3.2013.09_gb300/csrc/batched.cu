@@ -255,6 +255,11 @@ static int batch_setup(plsqr_ctx *ctx);
 
 static int batch_prepare(plsqr_ctx *ctx, int kp) {
   int rc;
+  if (ctx->lines_released) {
+    ctx_set_error(ctx, "the batched solver reads K by row and by column, which this context "
+                       "released (opts.lean)");
+    return PLSQR_ERR_STATE;
+  }
   if (!ctx->batch) {
     ctx->batch = new BatchState();
     if ((rc = batch_setup(ctx))) {

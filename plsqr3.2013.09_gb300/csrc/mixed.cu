@@ -29,10 +29,12 @@ constexpr int kThreads = 256;
 
 struct MixedState {
   float *k_hi = nullptr, *k_lo = nullptr, *kc_hi = nullptr;
-  // FP32 slab layouts (high half of the split, 6 bytes per nonzero) used by
-  // the inner sweeps when the FP64 context uses slabs
-  bool slabs = false;
+  // FP32 layouts of the high half of the split (6 bytes per nonzero) used by
+  // the inner sweeps: the unit layout (default) or the slab layout
+  bool slabs = false;  // either layout: slab partials added by the combine kernels
+  bool units = false;
   DevSlab<float> s_rows, s_cols;
+  DevUnitsT<float> u_rows, u_cols;
   float *uf = nullptr, *vf = nullptr, *wf = nullptr, *dxf = nullptr;
   double *dx = nullptr;  // FP64 correction of the FP64-vector inner sweeps
   bool v64 = false;      // inner sweeps keep u, v, w, dx in FP64 (slab products in FP32)
@@ -79,18 +81,34 @@ int mixed_prepare(plsqr_ctx *ctx) {
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->slab_ok) {
-    int slab = 24576;  // 96 KB of FP32 per block: two blocks per SM
-    if (const char *e = getenv("PLSQR_SLAB_SIZE_F"))
-      if (atoi(e) >= 1024 && atoi(e) <= 57344) slab = atoi(e);
-    // kernel rows: mostly consecutive columns, read by the lanes of a
-    // group in step (transposed chunks); columns: random rows, as stored
-    const int dyn = slab_dyn_blocks(ctx, true);
-    if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &M->s_rows,
-                                ctx->slab_group_f, dyn)) ||
-        (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &M->s_cols, 0,
-                                dyn)))
-      return rc;
-    if ((rc = slab_set_smem<float>(std::max(M->s_rows.smem, M->s_cols.smem)))) return rc;
+    // the unit layout on slabs of 49,152 FP32 values (192 KB, one 1,024-thread
+    // block per SM) unless PLSQR_MIXED_UNITS=0; PLSQR_UNIT_SIZE_F sets the slab
+    int uslab = 49152;
+    if (const char *e = getenv("PLSQR_UNIT_SIZE_F"))
+      if (atoi(e) >= 1024) uslab = atoi(e);
+    bool units = units_fit<float>(ctx->n, uslab) && units_fit<float>(ctx->m_k, uslab);
+    if (const char *e = getenv("PLSQR_MIXED_UNITS"))
+      if (atoi(e) == 0) units = false;
+    if (units) {
+      if ((rc = build_units<float>(ctx, ctx->K, ctx->n, uslab, &M->u_rows)) ||
+          (rc = build_units<float>(ctx, ctx->KC, ctx->m_k, uslab, &M->u_cols)))
+        return rc;
+      if ((rc = units_set_smem<float>(std::max(M->u_rows.smem, M->u_cols.smem)))) return rc;
+      M->units = true;
+    } else {
+      int slab = 24576;  // 96 KB of FP32 per block: two blocks per SM
+      if (const char *e = getenv("PLSQR_SLAB_SIZE_F"))
+        if (atoi(e) >= 1024 && atoi(e) <= 57344) slab = atoi(e);
+      // kernel rows: mostly consecutive columns, read by the lanes of a
+      // group in step (transposed chunks); columns: random rows, as stored
+      const int dyn = slab_dyn_blocks(ctx, true);
+      if ((rc = build_slab<float>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &M->s_rows,
+                                  ctx->slab_group_f, dyn)) ||
+          (rc = build_slab<float>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count, &M->s_cols,
+                                  0, dyn)))
+        return rc;
+      if ((rc = slab_set_smem<float>(std::max(M->s_rows.smem, M->s_cols.smem)))) return rc;
+    }
     M->slabs = true;
     const char *e = getenv("PLSQR_MIXED_F32VEC");
     M->v64 = !(e && atoi(e) == 1);
@@ -114,14 +132,39 @@ static CsrT<float> cols_f(const plsqr_ctx *ctx) {
 }
 // the inner sweeps' products: the FP64 kernels instantiated for FP32, on the
 // FP32 slabs when present
+// The FP32 kernel part of the inner products into slab partials (K v_f per
+// slab of v_f, K^T u_f per slab of u_f): the unit layout or the slab layout.
+static const float *rows_partials(plsqr_ctx *ctx, cudaStream_t s, int *n_slabs) {
+  MixedState *M = ctx->mixed;
+  if (M->units) {
+    units_spmv(M->u_rows, M->vf, s);
+    *n_slabs = M->u_rows.n_slabs;
+    return M->u_rows.partial;
+  }
+  slab_spmv(M->s_rows, ctx->slab_group_f, M->vf, s);
+  *n_slabs = M->s_rows.n_slabs;
+  return M->s_rows.partial;
+}
+static const float *cols_partials(plsqr_ctx *ctx, cudaStream_t s, int *n_slabs) {
+  MixedState *M = ctx->mixed;
+  if (M->units) {
+    units_spmv(M->u_cols, M->uf, s);
+    *n_slabs = M->u_cols.n_slabs;
+    return M->u_cols.partial;
+  }
+  slab_spmv(M->s_cols, ctx->slab_group_f, M->uf, s);
+  *n_slabs = M->s_cols.n_slabs;
+  return M->s_cols.partial;
+}
+
 static void m1f(plsqr_ctx *ctx, cudaStream_t s) {
   MixedState *M = ctx->mixed;
   if (M->slabs) {
-    const DevSlab<float> &S = M->s_rows;
-    slab_spmv(S, ctx->slab_group_f, M->vf, s);
+    int ns = 0;
+    const float *pp = rows_partials(ctx, s, &ns);
     k_combine_rows<float, float, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
-        S.partial, S.n_slabs, ctx->m_k, ctx->D.csr(), M->vf, M->uf, ctx->gc1k, kScaleNegAlpha,
-        ctx->st, ctx->parts_u);
+        pp, ns, ctx->m_k, ctx->D.csr(), M->vf, M->uf, ctx->gc1k, kScaleNegAlpha, ctx->st,
+        ctx->parts_u);
     return;
   }
   k_aprod1<float, kThreads, 2><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
@@ -131,11 +174,10 @@ static void m1f(plsqr_ctx *ctx, cudaStream_t s) {
 static void m2f(plsqr_ctx *ctx, cudaStream_t s, int mode) {
   MixedState *M = ctx->mixed;
   if (M->slabs) {
-    const DevSlab<float> &S = M->s_cols;
-    slab_spmv(S, ctx->slab_group_f, M->uf, s);
+    int ns = 0;
+    const float *pp = cols_partials(ctx, s, &ns);
     k_combine_cols<float, float, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
-        S.partial, S.n_slabs, ctx->n, ctx->DC.csr(), M->uf, ctx->m_k, M->vf, mode, ctx->st,
-        ctx->parts_v);
+        pp, ns, ctx->n, ctx->DC.csr(), M->uf, ctx->m_k, M->vf, mode, ctx->st, ctx->parts_v);
     return;
   }
   k_aprod2<float, kThreads, 2><<<ctx->g2, kThreads, 0, s>>>(
@@ -147,18 +189,16 @@ static void m2f(plsqr_ctx *ctx, cudaStream_t s, int mode) {
 // (written by the scaling kernels) with the FP32 slab matrix and combine the
 // FP32 partials into the FP64 vectors.
 static void m1v(plsqr_ctx *ctx, cudaStream_t s, int mode) {
-  MixedState *M = ctx->mixed;
-  slab_spmv(M->s_rows, ctx->slab_group_f, M->vf, s);
+  int ns = 0;
+  const float *pp = rows_partials(ctx, s, &ns);
   k_combine_rows<float, double, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
-      M->s_rows.partial, M->s_rows.n_slabs, ctx->m_k, ctx->D.csr(), ctx->v, ctx->u, ctx->gc1k,
-      mode, ctx->st, ctx->parts_u);
+      pp, ns, ctx->m_k, ctx->D.csr(), ctx->v, ctx->u, ctx->gc1k, mode, ctx->st, ctx->parts_u);
 }
 static void m2v(plsqr_ctx *ctx, cudaStream_t s, int mode) {
-  MixedState *M = ctx->mixed;
-  slab_spmv(M->s_cols, ctx->slab_group_f, M->uf, s);
+  int ns = 0;
+  const float *pp = cols_partials(ctx, s, &ns);
   k_combine_cols<float, double, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
-      M->s_cols.partial, M->s_cols.n_slabs, ctx->n, ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, mode,
-      ctx->st, ctx->parts_v);
+      pp, ns, ctx->n, ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, mode, ctx->st, ctx->parts_v);
 }
 
 static int enqueue_inner64(plsqr_ctx *ctx, cudaStream_t s) {

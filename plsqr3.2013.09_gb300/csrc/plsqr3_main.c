@@ -111,6 +111,8 @@ int main(int argc, char **argv) {
   o.precision = precision;
   o.verbose = verbose && precision == PLSQR_PREC_FP64;
   o.order = order;
+  /* one FP64 solve in the fast order needs only the unit layouts of K */
+  o.lean = precision == PLSQR_PREC_FP64 && order == PLSQR_ORDER_FAST;
   plsqr_ctx *ctx = NULL;
   int rc = plsqr_ctx_create_files(&f, &o, &ctx);
   if (rc) {

@@ -273,19 +273,31 @@ int slab_set_smem(size_t smem) {
 template int slab_set_smem<double>(size_t);
 template int slab_set_smem<float>(size_t);
 
-void units_spmv(const DevUnits &U, const double *x, cudaStream_t s) {
-  const UnitsArgs A{U.idx, U.val, U.slot0, U.q, U.c, U.line, U.unit_begin,
-                    U.n_lines, U.n_slabs, U.slab, U.n_idx};
+template <typename T>
+void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s) {
+  const UnitsArgs<T> A{U.idx,     U.val,     U.slot0,  U.q,     U.c,       U.line,       U.unit_begin,
+                       U.n_lines, U.n_slabs, U.slab,   U.n_idx, U.pf_dist, U.pf_pieces};
   cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
-  k_slab_units<1024><<<U.blocks, 1024, U.smem, s>>>(A, U.next, x, U.partial);
+  if (U.threads == 512)
+    k_slab_units<T, 512><<<U.blocks, 512, U.smem, s>>>(A, U.next, x, U.partial);
+  else
+    k_slab_units<T, 1024><<<U.blocks, 1024, U.smem, s>>>(A, U.next, x, U.partial);
 }
+template void units_spmv<double>(const DevUnitsT<double> &, const double *, cudaStream_t);
+template void units_spmv<float>(const DevUnitsT<float> &, const float *, cudaStream_t);
 
+template <typename T>
 int units_set_smem(size_t smem) {
-  return cudaFuncSetAttribute(k_slab_units<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)std::max<size_t>(smem, 1))
+  const int bytes = (int)std::max<size_t>(smem, 1);
+  return cudaFuncSetAttribute(k_slab_units<T, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              bytes) ||
+                 cudaFuncSetAttribute(k_slab_units<T, 512>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
              ? PLSQR_ERR_CUDA
              : PLSQR_OK;
 }
+template int units_set_smem<double>(size_t);
+template int units_set_smem<float>(size_t);
 
 static void m1(plsqr_ctx *ctx, cudaStream_t s, int mode, double *parts) {
   if (ctx->exact) {  // the reference's order (kernels_exact.cuh); no partial sums
@@ -345,7 +357,7 @@ static int slab_attrs(plsqr_ctx *ctx) {
   if (!ctx->use_slabs && !ctx->use_slabs_rows) return PLSQR_OK;
   int rc = slab_set_smem<double>(std::max(ctx->s_rows.smem, ctx->s_cols.smem));
   if (!rc && (ctx->use_units || ctx->use_units_rows))
-    rc = units_set_smem(std::max(ctx->u_cols.smem, ctx->u_rows.smem));
+    rc = units_set_smem<double>(std::max(ctx->u_cols.smem, ctx->u_rows.smem));
   if (rc) ctx_set_error(ctx, "cudaFuncSetAttribute failed for the slab kernels");
   return rc;
 }
@@ -608,6 +620,26 @@ void plsqr_ctx_destroy(plsqr_ctx *ctx) {
   delete ctx;
 }
 
+// opts.lean: the index and value arrays of K by row (by column) go once the
+// unit layout of the rows (columns) serves the FP64 product; the pointer
+// arrays stay (small, and read by the launch planning).
+static void release_kernel_lines(plsqr_ctx *ctx) {
+  if (ctx->use_units_rows) {
+    dev_free(ctx, ctx->K.idx);
+    dev_free(ctx, ctx->K.val);
+    ctx->K.idx = nullptr;
+    ctx->K.val = nullptr;
+    ctx->lines_released = true;
+  }
+  if (ctx->use_units) {
+    dev_free(ctx, ctx->KC.idx);
+    dev_free(ctx, ctx->KC.val);
+    ctx->KC.idx = nullptr;
+    ctx->KC.val = nullptr;
+    ctx->lines_released = true;
+  }
+}
+
 int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
                      const plsqr_sparse *d_csc, const plsqr_opts *opts, plsqr_ctx **out) {
   if (!out || !k_csc || !d_csr || !d_csc) return PLSQR_ERR_ARG;
@@ -628,6 +660,7 @@ int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
   if (ndev < 1 || o.device < 0 || o.device >= ndev) return PLSQR_ERR_NODEV;
   if (o.order != PLSQR_ORDER_FAST && o.order != PLSQR_ORDER_REFERENCE) return PLSQR_ERR_ARG;
   if (o.order == PLSQR_ORDER_REFERENCE && o.precision != PLSQR_PREC_FP64) return PLSQR_ERR_ARG;
+  if (o.lean && (o.order != PLSQR_ORDER_FAST || o.precision != PLSQR_PREC_FP64)) return PLSQR_ERR_ARG;
 
   plsqr_ctx *ctx = new plsqr_ctx();
   ctx->opts = o;
@@ -649,6 +682,7 @@ int plsqr_ctx_create(const plsqr_sparse *k_csc, const plsqr_sparse *d_csr,
     plsqr_ctx_destroy(ctx);
     return rc;
   }
+  if (o.lean) release_kernel_lines(ctx);
   *out = ctx;
   return PLSQR_OK;
 }

@@ -39,19 +39,24 @@ struct DevSlab {
   int chunk = 4;  // passes of lines a warp takes per counter grab
 };
 
-// The kernel matrix by column or by row in the unit layout (units.cuh).
-struct DevUnits {
+// The kernel matrix by column or by row in the unit layout (units.cuh);
+// FP64 values for the FP64 products, FP32 for the mixed solver's.
+template <typename T>
+struct DevUnitsT {
   uint16_t *idx = nullptr;
-  double *val = nullptr;
+  T *val = nullptr;
   int64_t *slot0 = nullptr;
   int32_t *q = nullptr, *c = nullptr, *line = nullptr, *unit_begin = nullptr;
   int32_t n_lines = 0, n_slabs = 0, slab = 0, n_idx = 0, n_units = 0;
+  int32_t threads = 1024;       // block size of k_slab_units: 1,024 or 512
+  int32_t pf_dist = 1, pf_pieces = 1;  // L2 prefetch of the unit kernel (set by build_units)
   int64_t slots = 0;
   int *next = nullptr;         // [n_slabs] unit counters, zeroed before every launch
-  double *partial = nullptr;   // [n_slabs * n_lines]
+  T *partial = nullptr;        // [n_slabs * n_lines]
   int blocks = 0;
   size_t smem = 0;
 };
+using DevUnits = DevUnitsT<double>;
 
 struct MixedState;  // mixed.cu
 struct BatchState;  // batched.cu
@@ -93,6 +98,7 @@ struct plsqr_ctx {
   DevUnits u_cols;                 // K by column in the unit layout
   bool use_units_rows = false;     // FP64 A x on the unit layout
   DevUnits u_rows;                 // K by row in the unit layout
+  bool lines_released = false;     // opts.lean freed K.idx/val or KC.idx/val
   int gc1k = 1, gc1d = 1, gc2 = 1;  // grids of the combine kernels
   BatchState *batch = nullptr;       // several right-hand sides (batched.cu)
   double *d_val0 = nullptr, *dc_val0 = nullptr;  // damping values before weighting
@@ -126,9 +132,18 @@ int build_slab(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, i
 // persistent grid or 0.
 int slab_dyn_blocks(const plsqr_ctx *ctx, bool fp32);
 int slab_plan(plsqr_ctx *ctx);
-int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevUnits *out);
+template <typename T>
+int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
+                DevUnitsT<T> *out);
+// slabs of `slab` entries over an index space of n_idx: few enough for the
+// build, 16-bit indices, and the slab and summing area of 1,024 threads in
+// shared memory
+template <typename T>
+bool units_fit(int32_t n_idx, int32_t slab);
 // plsqr_gpu.cu: unit product launch and its shared-memory attribute
-void units_spmv(const DevUnits &U, const double *x, cudaStream_t s);
+template <typename T>
+void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s);
+template <typename T>
 int units_set_smem(size_t smem);
 // plsqr_gpu.cu: slab product launch and its shared-memory attribute
 template <typename T>

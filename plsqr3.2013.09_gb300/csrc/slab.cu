@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "plsqr_internal.h"
@@ -134,7 +136,9 @@ template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, 
 // The unit layout (units.cuh) of a by-line matrix: segments counted as for
 // the slab layout, lines of each slab sorted longest segment first and cut
 // into units of kUnitLines, every unit's groups assigned to 32 lanes.
-int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, DevUnits *out) {
+template <typename T>
+int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
+                DevUnitsT<T> *out) {
   const int n_lines = L.n_lines;
   const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
   if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
@@ -203,7 +207,7 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, 
     return rc;
   CK(cudaMemsetAsync(out->idx, 0, sizeof(uint16_t) * 8 * (size_t)std::max<int64_t>(slots, 1),
                      ctx->stream));
-  CK(cudaMemsetAsync(out->val, 0, sizeof(double) * 8 * (size_t)std::max<int64_t>(slots, 1),
+  CK(cudaMemsetAsync(out->val, 0, sizeof(T) * 8 * (size_t)std::max<int64_t>(slots, 1),
                      ctx->stream));
   CK(cudaMemcpy(out->slot0, uslot.data(), sizeof(int64_t) * uslot.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(out->q, uq.data(), sizeof(int32_t) * uq.size(), cudaMemcpyHostToDevice));
@@ -213,24 +217,56 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab, 
   CK(cudaMemcpy(d_seg_unit, seg_unit.data(), sizeof(int32_t) * seg_unit.size(),
                 cudaMemcpyHostToDevice));
   CK(cudaMemcpy(d_seg_pos, seg_pos.data(), sizeof(int32_t) * seg_pos.size(), cudaMemcpyHostToDevice));
-  const UnitsArgs U{out->idx, out->val, out->slot0, out->q, out->c, out->line, out->unit_begin,
-                    n_lines, n_slabs, slab, n_idx};
+  const UnitsArgs<T> U{out->idx,       out->val, out->slot0, out->q, out->c, out->line,
+                       out->unit_begin, n_lines,  n_slabs,    slab,   n_idx,  0,
+                       0};
   k_units_fill<<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, L.val, n_lines, n_slabs, slab, d_seg_unit,
                                            d_seg_pos, U, out->idx, out->val);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   dev_free(ctx, d_seg_unit);
   dev_free(ctx, d_seg_pos);
-  out->blocks = ctx->sm_count;
-  out->smem = units_smem((size_t)std::min(slab, n_idx), 1024);
+  // PLSQR_UNIT_THREADS=512: two blocks per SM where two slabs fit in shared memory
+  out->threads = 1024;
+  if (const char *e = getenv("PLSQR_UNIT_THREADS"))
+    if (atoi(e) == 512 &&
+        2 * (units_smem<T>((size_t)std::min(slab, n_idx), 512) + 1024) <= 228 * 1024)
+      out->threads = 512;
+  out->blocks = ctx->sm_count * (1024 / out->threads);
+  // Each lane prefetches all its loads of the next step into L2 (on the
+  // 96x96x32 problem against the step after next, first value piece only:
+  // FP64 A x 2.32 -> 2.29 ms, FP32 A x 1.28 -> 1.22 ms; two steps of all
+  // pieces are on par, four or more steps of all pieces slower: 4,864 warps
+  // prefetching 10 KB each begin to evict one another's lines from L2).
+  // PLSQR_UNIT_PREFETCH=d,p: d steps ahead (0: none), p value pieces.
+  out->pf_dist = 1;
+  out->pf_pieces = UnitPieces<T>::P;
+  if (const char *e = getenv("PLSQR_UNIT_PREFETCH")) {
+    int d = 1, pc = UnitPieces<T>::P;
+    if (sscanf(e, "%d,%d", &d, &pc) >= 1 && d >= 0 && d <= 16) out->pf_dist = d;
+    if (pc >= 1 && pc <= UnitPieces<T>::P) out->pf_pieces = pc;
+  }
+  out->smem = units_smem<T>((size_t)std::min(slab, n_idx), out->threads);
   return PLSQR_OK;
 }
+template int build_units<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
+                                 DevUnitsT<double> *);
+
+template <typename T>
+bool units_fit(int32_t n_idx, int32_t slab) {
+  return slab >= 1 && slab <= 65536 && (n_idx + slab - 1) / slab <= kMaxSlabs &&
+         units_smem<T>((size_t)std::min(slab, n_idx), 1024) <= 227 * 1024;
+}
+template bool units_fit<double>(int32_t, int32_t);
+template bool units_fit<float>(int32_t, int32_t);
+template int build_units<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
+                                DevUnitsT<float> *);
 
 // Plan the slab paths.  slab_ok: every dimension fits kMaxSlabs slabs of
-// 24,576 FP32 values, so the mixed solver's inner products use FP32 slabs.
-// FP64: both products on slabs of 24,576 values in the unit layout
-// (units.cuh): on the 96x96x32 problem A^T y 2.66 -> 2.30 ms and A x 2.57 ->
-// 2.31 ms against the segment-per-group slab kernel and the per-row kernel
+// 24,576 FP32 values, so the mixed solver's inner products use FP32 layouts.
+// FP64: both products on slabs of 20,480 values in the unit layout
+// (units.cuh): on the 96x96x32 problem A^T y 2.66 -> 2.26 ms and A x 2.57 ->
+// 2.29 ms against the segment-per-group slab kernel and the per-row kernel
 // k_aprod1 (16-bit indices, every lane busy, the gathered vector in shared
 // memory).  PLSQR_SLABS overrides: 0 none, 1 both orientations (default),
 // 2 A^T y only; PLSQR_SLAB_UNITS=0 the slab kernel instead of the units.
@@ -243,9 +279,11 @@ int slab_plan(plsqr_ctx *ctx) {
   ctx->gc1k = std::max(1, std::min({sm * 2, (ctx->m_k + 255) / 256, half}));
   ctx->gc1d = std::max(1, std::min({sm * 2, (ctx->m_d + 255) / 256, half}));
   ctx->gc2 = std::max(1, std::min({sm * 4, (ctx->n + 255) / 256, kMaxParts}));
-  int mode = 1;
+  // a mixed-precision context solves with its FP32 layouts (mixed.cu) and
+  // runs FP64 products only for plsqr_aprod calls: no FP64 layouts by default
+  int mode = ctx->opts.precision == PLSQR_PREC_MIXED ? 0 : 1;
   if (const char *e = getenv("PLSQR_SLABS")) mode = atoi(e);
-  int slab = 24576;  // 192 KB of FP64 per block
+  int slab = 20480;  // 160 KB of FP64 per block (24,576: A x + A^T y 1.5% slower)
   if (const char *s = getenv("PLSQR_SLAB_SIZE"))
     if (atoi(s) >= 1024 && atoi(s) <= 28672) slab = atoi(s);
   const bool rows_fit = (ctx->n + slab - 1) / slab <= kMaxSlabs;
@@ -257,7 +295,7 @@ int slab_plan(plsqr_ctx *ctx) {
   int units = 1;
   if (const char *e = getenv("PLSQR_SLAB_UNITS")) units = atoi(e) != 0;
   if (mode == 1 && rows_fit) {
-    if (units && units_smem((size_t)std::min(slab, ctx->n), 1024) <= 227 * 1024) {
+    if (units && units_smem<double>((size_t)std::min(slab, ctx->n), 1024) <= 227 * 1024) {
       if ((rc = build_units(ctx, ctx->K, ctx->n, slab, &ctx->u_rows))) return rc;
       ctx->use_units_rows = true;
     } else if ((rc = build_slab<double>(ctx, ctx->K, ctx->n, slab, 16 * ctx->sm_count, &ctx->s_rows,
@@ -267,7 +305,7 @@ int slab_plan(plsqr_ctx *ctx) {
     ctx->use_slabs_rows = true;
   }
   if ((mode == 1 || mode == 2) && cols_fit) {
-    if (units && units_smem((size_t)std::min(slab, ctx->m_k), 1024) <= 227 * 1024) {
+    if (units && units_smem<double>((size_t)std::min(slab, ctx->m_k), 1024) <= 227 * 1024) {
       if ((rc = build_units(ctx, ctx->KC, ctx->m_k, slab, &ctx->u_cols))) return rc;
       ctx->use_units = true;
     } else if ((rc = build_slab<double>(ctx, ctx->KC, ctx->m_k, slab, 16 * ctx->sm_count,

@@ -14,9 +14,11 @@
 // every step the 32 lanes read 32 consecutive slots:
 //
 //   idx[(slot0 + k*32 + j) * 8 + e]              uint16, entry e of the group
-//   val[(slot0*4 + (k*4 + p)*32 + j) * 2 + w]    FP64, entry e = 2p + w
+//   val[(slot0*P + (k*P + p)*32 + j) * E + w]    entry e = E p + w
 //
-// (four coalesced 16-byte loads of the values per step).  A lane sums its
+// with E = 16 / sizeof(T) values per 16-byte piece and P = 8 / E pieces per
+// group: FP64 four pieces of two, FP32 (the mixed solver's inner products)
+// two of four, coalesced 16-byte loads either way.  A lane sums its
 // groups into the line they belong to; a line wholly inside one lane's run
 // is written by that lane, and a line spread over lanes is summed by the
 // unit's lane of the same index, from the lanes' parts in lane order, so the
@@ -30,25 +32,37 @@ namespace plsqr {
 
 constexpr int kUnitLines = 32;  // lines per unit: one per lane of the summing step
 
+template <typename T>
 struct UnitsArgs {
   const uint16_t *idx;         // [slots * 8]
-  const double *val;           // [slots * 8]
+  const T *val;                // [slots * 8]
   const int64_t *slot0;        // [units] first slot of each unit
   const int32_t *q;            // [units] groups per lane
   const int32_t *c;            // [units * (kUnitLines + 1)] first group of each line in the unit's stream
   const int32_t *line;         // [units * kUnitLines] line index, -1 past the slab's last line
   const int32_t *unit_begin;   // [n_slabs + 1] first unit of each slab
   int32_t n_lines, n_slabs, slab, n_idx;
+  int32_t pf_dist;    // steps ahead of the L2 prefetch (0: none)
+  int32_t pf_pieces;  // value pieces prefetched per lane: 1 or all P
+};
+
+// Values per 16-byte piece of a group, and pieces per group.
+template <typename T>
+struct UnitPieces {
+  static constexpr int E = 16 / (int)sizeof(T);
+  static constexpr int P = 8 / E;
 };
 
 // Setup: entry o of segment (s, l) to its slot.  seg_unit / seg_pos give
 // the unit of segment (s, l) and the line's position in it; the arrays were
-// zeroed, so padding slots and entries stay (index 0, value 0).
-static __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__restrict__ idx,
-                                    const double *__restrict__ val, int n_lines, int n_slabs,
-                                    int slab, const int32_t *__restrict__ seg_unit,
-                                    const int32_t *__restrict__ seg_pos, UnitsArgs U,
-                                    uint16_t *__restrict__ sidx, double *__restrict__ sval) {
+// zeroed, so padding slots and entries stay (index 0, value 0).  FP32
+// values are the FP64 ones rounded to nearest.
+template <typename T>
+__global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__restrict__ idx,
+                             const double *__restrict__ val, int n_lines, int n_slabs, int slab,
+                             const int32_t *__restrict__ seg_unit, const int32_t *__restrict__ seg_pos,
+                             UnitsArgs<T> U, uint16_t *__restrict__ sidx, T *__restrict__ sval) {
+  constexpr int E = UnitPieces<T>::E, P = UnitPieces<T>::P;
   for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n_lines; l += gridDim.x * blockDim.x) {
     int64_t cur[64];
     for (int s = 0; s < n_slabs; ++s) cur[s] = 0;
@@ -63,23 +77,93 @@ static __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32
       const int64_t base = U.slot0[u];
       const int w = (int)(o & 7);
       sidx[(base + k * 32 + j) * 8 + w] = (uint16_t)(idx[e] - s * slab);
-      sval[(base * 4 + (k * 4 + w / 2) * 32 + j) * 2 + (w & 1)] = val[e];
+      sval[(base * P + (k * P + w / E) * 32 + j) * E + w % E] = (T)val[e];
     }
   }
 }
 
 // partial[s * n_lines + l] = sum over segment (s, l) of val * x_slab[idx].
-// One block per SM (the 192 KB slab of x plus the summing area); the unit's
-// loads for the step after next are prefetched into L2.
-template <int kThreads>
-__global__ void __launch_bounds__(kThreads, 1)
-    k_slab_units(UnitsArgs A, int *__restrict__ next, const double *__restrict__ x,
-                 double *__restrict__ partial) {
+// 1,024 threads: one block per SM (the 192 KB slab of x plus the summing
+// area); 512 threads: two blocks per SM on slabs of up to 12,288 entries.
+// Each lane prefetches its loads of a later step into L2 (by default all
+// of the next step's).
+// One step of a lane: its group's 8 values (P coalesced 16-byte loads).
+__device__ __forceinline__ void unit_vals(const double *val, int64_t base, int k, int lane,
+                                          double (&v)[8]) {
+  const double2 *p = reinterpret_cast<const double2 *>(val) + base * 4 + (int64_t)(k * 4) * 32 + lane;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const double2 a = __ldg(p + 32 * i);
+    v[2 * i] = a.x;
+    v[2 * i + 1] = a.y;
+  }
+}
+__device__ __forceinline__ void unit_vals(const float *val, int64_t base, int k, int lane,
+                                          float (&v)[8]) {
+  const float4 *p = reinterpret_cast<const float4 *>(val) + base * 2 + (int64_t)(k * 2) * 32 + lane;
+  const float4 a = __ldg(p), b = __ldg(p + 32);
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+  v[4] = b.x;
+  v[5] = b.y;
+  v[6] = b.z;
+  v[7] = b.w;
+}
+
+// A lane's running sum of one line.  FP64 values: two chains of fused
+// multiply-adds.  FP32 values (the mixed solver): each group's 8 products
+// summed in FP32, the group sums added in FP64, so that a line of thousands
+// of entries streamed by one lane keeps FP64 accuracy in its sum (a plain
+// FP32 running sum cost the mixed solver 7% more iterations to 1e-6 on the
+// 96x96x32 problem); the FP64 pipe is otherwise idle in the FP32 product.
+template <typename T>
+struct UnitSum;
+template <>
+struct UnitSum<double> {
+  double a0 = 0.0, a1 = 0.0;
+  __device__ __forceinline__ void add8(const double (&v)[8], const double *xs, uint4 g) {
+    a0 = fma(v[0], xs[g.x & 0xffff], a0);
+    a1 = fma(v[1], xs[g.x >> 16], a1);
+    a0 = fma(v[2], xs[g.y & 0xffff], a0);
+    a1 = fma(v[3], xs[g.y >> 16], a1);
+    a0 = fma(v[4], xs[g.z & 0xffff], a0);
+    a1 = fma(v[5], xs[g.z >> 16], a1);
+    a0 = fma(v[6], xs[g.w & 0xffff], a0);
+    a1 = fma(v[7], xs[g.w >> 16], a1);
+  }
+  __device__ __forceinline__ double total() const { return a0 + a1; }
+  __device__ __forceinline__ void reset() { a0 = a1 = 0.0; }
+};
+template <>
+struct UnitSum<float> {
+  double a = 0.0;
+  __device__ __forceinline__ void add8(const float (&v)[8], const float *xs, uint4 g) {
+    float g0 = v[0] * xs[g.x & 0xffff], g1 = v[1] * xs[g.x >> 16];
+    g0 = fmaf(v[2], xs[g.y & 0xffff], g0);
+    g1 = fmaf(v[3], xs[g.y >> 16], g1);
+    g0 = fmaf(v[4], xs[g.z & 0xffff], g0);
+    g1 = fmaf(v[5], xs[g.z >> 16], g1);
+    g0 = fmaf(v[6], xs[g.w & 0xffff], g0);
+    g1 = fmaf(v[7], xs[g.w >> 16], g1);
+    a += (double)(g0 + g1);
+  }
+  __device__ __forceinline__ double total() const { return a; }
+  __device__ __forceinline__ void reset() { a = 0.0; }
+};
+
+template <typename T, int kThreads>
+__global__ void __launch_bounds__(kThreads, 1024 / kThreads)
+    k_slab_units(UnitsArgs<T> A, int *__restrict__ next, const T *__restrict__ x,
+                 T *__restrict__ partial) {
+  constexpr int P = UnitPieces<T>::P;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double *xs = reinterpret_cast<double *>(smem_raw);
-  // per warp: each lane's first and last line and its sums for them, after
-  // the slab (min(slab, n_idx) entries: the size the launch gives)
-  double *pf_all = xs + min(A.slab, A.n_idx);
+  T *xs = reinterpret_cast<T *>(smem_raw);
+  // per warp: each lane's first and last line and its FP64 sums for them,
+  // after the slab (min(slab, n_idx) entries: the size the launch gives,
+  // rounded up to 2 so that the sums after an FP32 slab stay aligned)
+  double *pf_all = reinterpret_cast<double *>(xs + ((min(A.slab, A.n_idx) + 1) & ~1));
   double *pl_all = pf_all + kThreads;
   int *lf_all = reinterpret_cast<int *>(pl_all + kThreads);
   int *ll_all = lf_all + kThreads;
@@ -88,7 +172,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   double *pf = pf_all + warp * 32, *pl = pl_all + warp * 32;
   int *lf = lf_all + warp * 32, *ll = ll_all + warp * 32;
   const uint4 *idx8 = reinterpret_cast<const uint4 *>(A.idx);
-  const double2 *val2 = reinterpret_cast<const double2 *>(A.val);
+  const uint4 *val16 = reinterpret_cast<const uint4 *>(A.val);
   int s = (int)(((int64_t)blockIdx.x * A.n_slabs) / gridDim.x);
   for (int visit = 0; visit < A.n_slabs; ++visit, s = (s + 1 == A.n_slabs) ? 0 : s + 1) {
     const int u0 = A.unit_begin[s], nu = A.unit_begin[s + 1] - u0;
@@ -101,7 +185,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int len = (int)min((int64_t)A.slab, (int64_t)A.n_idx - xbase);
     for (int i = threadIdx.x; i < len; i += kThreads) xs[i] = x[xbase + i];
     __syncthreads();
-    double *part = partial + (int64_t)s * A.n_lines;
+    T *part = partial + (int64_t)s * A.n_lines;
     for (;;) {
       int u = 0;
       if (lane == 0) u = atomicAdd(next + s, 1);
@@ -121,38 +205,34 @@ __global__ void __launch_bounds__(kThreads, 1)
         nb = c[li + 1];
       }
       const int li_first = li;
-      double acc0 = 0.0, acc1 = 0.0, p_first = 0.0, p_last = 0.0;
+      UnitSum<T> acc;
+      double p_first = 0.0, p_last = 0.0;
       int li_last = kUnitLines;
       for (int k = 0; k < q; ++k) {
         const int t = sj + k;
         if (t == nb && t < G) {  // this lane's run enters the next line
-          const double a = acc0 + acc1;
+          const double a = acc.total();
           if (li == li_first) p_first = a;
-          else part[ln[li]] = a;  // a line wholly inside the run
-          acc0 = acc1 = 0.0;
+          else part[ln[li]] = (T)a;  // a line wholly inside the run
+          acc.reset();
           ++li;
           while (c[li + 1] <= t) ++li;
           nb = c[li + 1];
         }
-        if (k + 2 < q) {  // the step after next into L2
-          asm volatile("prefetch.global.L2 [%0];" ::"l"(idx8 + base + (int64_t)(k + 2) * 32 + lane));
-          asm volatile("prefetch.global.L2 [%0];" ::"l"(val2 + base * 4 +
-                                                        (int64_t)((k + 2) * 4) * 32 + lane));
+        const int kp = k + A.pf_dist;
+        if (A.pf_dist > 0 && kp < q) {  // a later step into L2
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(idx8 + base + (int64_t)kp * 32 + lane));
+          for (int pc = 0; pc < A.pf_pieces; ++pc)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(val16 + base * P +
+                                                          (int64_t)(kp * P + pc) * 32 + lane));
         }
         const uint4 g = __ldg(idx8 + base + (int64_t)k * 32 + lane);
-        const double2 *vp = val2 + base * 4 + (int64_t)(k * 4) * 32 + lane;
-        const double2 v0 = __ldg(vp), v1 = __ldg(vp + 32), v2 = __ldg(vp + 64), v3 = __ldg(vp + 96);
-        acc0 = fma(v0.x, xs[g.x & 0xffff], acc0);
-        acc1 = fma(v0.y, xs[g.x >> 16], acc1);
-        acc0 = fma(v1.x, xs[g.y & 0xffff], acc0);
-        acc1 = fma(v1.y, xs[g.y >> 16], acc1);
-        acc0 = fma(v2.x, xs[g.z & 0xffff], acc0);
-        acc1 = fma(v2.y, xs[g.z >> 16], acc1);
-        acc0 = fma(v3.x, xs[g.w & 0xffff], acc0);
-        acc1 = fma(v3.y, xs[g.w >> 16], acc1);
+        T v[8];
+        unit_vals(A.val, base, k, lane, v);
+        acc.add8(v, xs, g);
       }
       if (sj < G) {
-        const double a = acc0 + acc1;
+        const double a = acc.total();
         if (li == li_first) {
           p_first = a;
         } else {
@@ -170,13 +250,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (l >= 0) {
         const int c0 = c[lane], c1 = c[lane + 1];
         if (c0 == c1) {
-          part[l] = 0.0;
+          part[l] = 0;
         } else {
           const int a = c0 / q, b = (c1 - 1) / q;
           if (a != b || lf[a] == lane || ll[a] == lane) {
             double t = lf[a] == lane ? pf[a] : pl[a];
             for (int j = a + 1; j <= b; ++j) t += lf[j] == lane ? pf[j] : pl[j];
-            part[l] = t;
+            part[l] = (T)t;
           }
         }
       }
@@ -186,9 +266,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Shared memory of k_slab_units: the slab plus 24 bytes per thread.
+// Shared memory of k_slab_units: the slab plus 2 FP64 sums and 2 line
+// indices per thread.
+template <typename T>
 __host__ __device__ constexpr size_t units_smem(size_t slab_entries, int threads) {
-  return slab_entries * sizeof(double) + (size_t)threads * (2 * sizeof(double) + 2 * sizeof(int));
+  return ((slab_entries + 1) & ~size_t(1)) * sizeof(T) +
+         (size_t)threads * (2 * sizeof(double) + 2 * sizeof(int));
 }
 
 }  // namespace plsqr

@@ -42,7 +42,10 @@ static int make_ctx(PPDataV3_TRI *p) {
   plsqr_sparse dcs = {dc->numRow, dc->numCol, dc->numNonzero, dc->col_ptr, NULL, dc->row_idx,
                       dc->val};
   static int at_exit;
-  const int rc = plsqr_ctx_create(&ks, &ds, &dcs, NULL, &g_ctx);
+  plsqr_opts o;
+  plsqr_default_opts(&o);
+  o.lean = 1; /* the operator alone: the unit layouts of K are all it reads */
+  const int rc = plsqr_ctx_create(&ks, &ds, &dcs, &o, &g_ctx);
   /* registered after the CUDA runtime has started, so that it runs first */
   if (rc == PLSQR_OK && !at_exit) at_exit = atexit(release_ctx) == 0;
   return rc;

@@ -31,7 +31,7 @@ def _f64(a, n, name):
 class Context:
     def __init__(self, problem: Problem | None = None, *, files: dict | None = None,
                  precision: str = "fp64", device: int = 0, use_graph: bool = True,
-                 verbose: bool = False, grid=None, order: str = "fast"):
+                 verbose: bool = False, grid=None, order: str = "fast", lean: bool = False):
         L = N.lib()
         o = N.Opts()
         L.plsqr_default_opts(C.byref(o))
@@ -42,6 +42,7 @@ class Context:
         if order not in ("fast", "reference"):
             raise ValueError("order must be 'fast' or 'reference'")
         o.order = N.ORDER_REFERENCE if order == "reference" else N.ORDER_FAST
+        o.lean = int(lean)  # release K by row / by column once the unit layouts hold them
         if grid is None and problem is not None:
             grid = problem.meta.get("grid")
         if grid is not None:

@@ -36,6 +36,7 @@ FP64_CASES = [
     {"PLSQR_SLABS": "2", "PLSQR_UNROLL": "1"},
     {"PLSQR_SLABS": "2", "PLSQR_UNROLL": "4"},
     {"PLSQR_SLABS": "2", "PLSQR_BLOCKS_PER_SM": "1"},
+    {"PLSQR_UNIT_THREADS": "512", "PLSQR_SLAB_SIZE": "12288"},  # two unit blocks per SM
     {"PLSQR_NATURAL_ORDER": "1", "PLSQR_SLABS": "0"},
 ]
 
@@ -55,11 +56,16 @@ def test_fp64_switches_match_reference(env, pkg, problems, monkeypatch):
 
 
 MIXED_CASES = [
+    {},                                                     # FP32 unit layout (default)
     {"PLSQR_MIXED_F32VEC": "1"},                            # FP32 vectors in the inner sweeps
-    {"PLSQR_SLAB_SIZE_F": "1024"},
-    {"PLSQR_SLAB_GROUP_F": "4"},                            # transposed chunks of other widths
-    {"PLSQR_SLAB_GROUP_F": "8"},
-    {"PLSQR_SLAB_GROUP_F": "32"},
+    {"PLSQR_UNIT_SIZE_F": "1024"},                          # many slabs, short segments
+    {"PLSQR_UNIT_SIZE_F": "24576", "PLSQR_UNIT_THREADS": "512"},  # two blocks per SM
+    {"PLSQR_MIXED_UNITS": "0"},                             # FP32 slab kernels
+    {"PLSQR_MIXED_UNITS": "0", "PLSQR_MIXED_F32VEC": "1"},
+    {"PLSQR_MIXED_UNITS": "0", "PLSQR_SLAB_SIZE_F": "1024"},
+    {"PLSQR_MIXED_UNITS": "0", "PLSQR_SLAB_GROUP_F": "4"},  # transposed chunks of other widths
+    {"PLSQR_MIXED_UNITS": "0", "PLSQR_SLAB_GROUP_F": "8"},
+    {"PLSQR_MIXED_UNITS": "0", "PLSQR_SLAB_GROUP_F": "32"},
     {"PLSQR_SLABS": "0"},
 ]
 
