@@ -446,8 +446,10 @@ def time_to_tol(pkg, prob, ctx64, iters, tol) -> dict:
             run = dict(sweeps=1, inner=k) if sweeps == 1 else dict(sweeps=sweeps, inner=inner)
             t = [cm.lsqr(**run)["result"]["seconds_total"] for _ in range(3)]
             out["mixed"] = {**run, "inner_iterations_to_tol": k, "seconds": min(t),
-                            "form": "FP32 products on the hi half of the value split, FP64 "
-                                    "vectors, norms and recurrence; FP64 residual refinement"}
+                            "form": "FP32 values (the hi half of the value split) times hi + lo "
+                                    "FP32 pairs of the FP64 vectors, error-free FP32 products "
+                                    "and sums, FP64 slab partials; FP64 vectors, norms and "
+                                    "recurrence; FP64 residual refinement"}
             if "seconds" in out["fp64"]:
                 out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds"] / min(t)
         else:

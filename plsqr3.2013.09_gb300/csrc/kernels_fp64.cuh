@@ -227,11 +227,13 @@ __global__ void __launch_bounds__(kThreads)
 __device__ __forceinline__ double scale_elem(double x, double r) { return dmul(x, r); }
 __device__ __forceinline__ float scale_elem(float x, double r) { return x * (float)r; }
 
-// mirror (optional): FP32 copy of the scaled u, gathered by FP32 products.
+// mirror (optional): FP32 copy of the scaled u, gathered by FP32 products;
+// mirror_lo (optional): the rest, u - mirror rounded to FP32.
 template <typename T, int kThreads>
 __global__ void __launch_bounds__(kThreads)
     k_norm_u(T *__restrict__ u, int64_t m, const double *__restrict__ parts, int gk, int gd,
-             DevState *__restrict__ st, int start, float *__restrict__ mirror = nullptr) {
+             DevState *__restrict__ st, int start, float *__restrict__ mirror = nullptr,
+             float *__restrict__ mirror_lo = nullptr) {
   __shared__ double smem[kThreads / 32];
   __shared__ double s_rb;
   const double sk = sum_parts<kThreads>(parts, gk, smem);
@@ -256,7 +258,11 @@ __global__ void __launch_bounds__(kThreads)
        i += (int64_t)gridDim.x * kThreads) {
     const T y = scale_elem(u[i], rb);
     u[i] = y;
-    if (mirror) mirror[i] = (float)y;
+    if (mirror) {
+      const float h = (float)y;
+      mirror[i] = h;
+      if (mirror_lo) mirror_lo[i] = (float)((double)y - (double)h);
+    }
   }
 }
 
@@ -317,7 +323,7 @@ __global__ void __launch_bounds__(kThreads)
                const double *__restrict__ parts, int gp, DevState *__restrict__ st,
                double *__restrict__ parts_dk, double *__restrict__ parts_err,
                plsqr_iter *__restrict__ hist, int start, float *__restrict__ v_mirror = nullptr,
-               const double *__restrict__ x_base = nullptr) {
+               const double *__restrict__ x_base = nullptr, float *__restrict__ v_mirror_lo = nullptr) {
   __shared__ double smem[kThreads / 32];
   __shared__ double s_alpha, s_ra;
   __shared__ Step s_step;
@@ -338,7 +344,11 @@ __global__ void __launch_bounds__(kThreads)
       double vi = v[i];
       if (ra != 0.0) vi = dmul(vi, ra);
       v[i] = vi;
-      if (v_mirror) v_mirror[i] = (float)vi;
+      if (v_mirror) {
+        const float h = (float)vi;
+        v_mirror[i] = h;
+        if (v_mirror_lo) v_mirror_lo[i] = (float)(vi - (double)h);
+      }
       w[i] = ra != 0.0 ? vi : 0.0;  // w = v only when alpha > 0 (lsqr.c:392-395)
       x[i] = 0.0;
       if (se) se[i] = 0.0;
@@ -379,7 +389,11 @@ __global__ void __launch_bounds__(kThreads)
       vi = dmul(vi, ra);
       v[i] = vi;
     }
-    if (v_mirror) v_mirror[i] = (float)vi;
+    if (v_mirror) {
+      const float h = (float)vi;
+      v_mirror[i] = h;
+      if (v_mirror_lo) v_mirror_lo[i] = (float)(vi - (double)h);
+    }
     const double t = w[i];
     const double xi = dadd(dmul(sp.t1, t), x[i]);
     x[i] = xi;

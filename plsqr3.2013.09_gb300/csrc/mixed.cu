@@ -35,6 +35,11 @@ struct MixedState {
   bool units = false;
   DevSlab<float> s_rows, s_cols;
   DevUnitsT<float> u_rows, u_cols;
+  // the unit products gather the FP32 pairs (mirror, mirror_lo) with
+  // error-free products and sums (units.cuh; PLSQR_MIXED_HILO=0: the mirror
+  // alone)
+  bool hilo = false;
+  float *uf_lo = nullptr, *vf_lo = nullptr;
   float *uf = nullptr, *vf = nullptr, *wf = nullptr, *dxf = nullptr;
   double *dx = nullptr;  // FP64 correction of the FP64-vector inner sweeps
   bool v64 = false;      // inner sweeps keep u, v, w, dx in FP64 (slab products in FP32)
@@ -83,16 +88,31 @@ int mixed_prepare(plsqr_ctx *ctx) {
   if (ctx->slab_ok) {
     // the unit layout on slabs of 49,152 FP32 values (192 KB, one 1,024-thread
     // block per SM) unless PLSQR_MIXED_UNITS=0; PLSQR_UNIT_SIZE_F sets the slab
-    int uslab = 49152;
+    // hi + lo mirrors with error-free products and sums unless
+    // PLSQR_MIXED_HILO=0: on the 96x96x32 problem 381 inner iterations to
+    // 1e-6 (FP64: 376) at 2.62 ms against 422 at 2.48 ms with the plain FP32
+    // mirror, whose rounding, and the products', the solver otherwise pays
+    // for in iterations
+    const char *eh = getenv("PLSQR_MIXED_HILO");
+    const bool hilo = !(eh && atoi(eh) == 0);
+    int uslab = hilo ? 24576 : 49152;  // 192 KB of FP32 pairs or of FP32 values
     if (const char *e = getenv("PLSQR_UNIT_SIZE_F"))
       if (atoi(e) >= 1024) uslab = atoi(e);
-    bool units = units_fit<float>(ctx->n, uslab) && units_fit<float>(ctx->m_k, uslab);
+    bool units = units_fit<float>(ctx->n, uslab, hilo) && units_fit<float>(ctx->m_k, uslab, hilo);
     if (const char *e = getenv("PLSQR_MIXED_UNITS"))
       if (atoi(e) == 0) units = false;
     if (units) {
-      if ((rc = build_units<float>(ctx, ctx->K, ctx->n, uslab, &M->u_rows)) ||
-          (rc = build_units<float>(ctx, ctx->KC, ctx->m_k, uslab, &M->u_cols)))
+      if ((rc = build_units<float>(ctx, ctx->K, ctx->n, uslab, &M->u_rows, hilo)) ||
+          (rc = build_units<float>(ctx, ctx->KC, ctx->m_k, uslab, &M->u_cols, hilo)))
         return rc;
+      if (hilo) {
+        if ((rc = dev_alloc(ctx, &M->uf_lo, (size_t)m)) ||
+            (rc = dev_alloc(ctx, &M->vf_lo, (size_t)ctx->n)))
+          return rc;
+        CK(cudaMemsetAsync(M->uf_lo, 0, sizeof(float) * m, ctx->stream));
+        CK(cudaMemsetAsync(M->vf_lo, 0, sizeof(float) * ctx->n, ctx->stream));
+      }
+      M->hilo = hilo;
       if ((rc = units_set_smem<float>(std::max(M->u_rows.smem, M->u_cols.smem)))) return rc;
       M->units = true;
     } else {
@@ -130,41 +150,49 @@ static CsrT<float> rows_f(const plsqr_ctx *ctx) {
 static CsrT<float> cols_f(const plsqr_ctx *ctx) {
   return CsrT<float>{ctx->KC.ptr, ctx->KC.idx, ctx->mixed->kc_hi, ctx->KC.n_lines};
 }
-// the inner sweeps' products: the FP64 kernels instantiated for FP32, on the
-// FP32 slabs when present
-// The FP32 kernel part of the inner products into slab partials (K v_f per
-// slab of v_f, K^T u_f per slab of u_f): the unit layout or the slab layout.
-static const float *rows_partials(plsqr_ctx *ctx, cudaStream_t s, int *n_slabs) {
+// The inner sweeps' products.  The FP32 kernel part into slab partials (K v_f
+// per slab of v_f, K^T u_f per slab of u_f): on the unit layout (FP64
+// partials: each line's slab sum kept to FP64, a rounding to FP32 there cost
+// as many iterations as the FP32 mirror) or the slab layout (FP32
+// partials); then the combine kernel with the damping part and the scaling,
+// into the FP32 vectors (m1f, m2f) or the FP64 ones (m1v, m2v).  Without
+// slabs: the per-line kernels instantiated for FP32.
+template <typename TV>
+static void combine_rows(plsqr_ctx *ctx, cudaStream_t s, const TV *v, TV *u, int mode) {
   MixedState *M = ctx->mixed;
+  const int g = ctx->gc1k + ctx->gc1d;
   if (M->units) {
-    units_spmv(M->u_rows, M->vf, s);
-    *n_slabs = M->u_rows.n_slabs;
-    return M->u_rows.partial;
+    units_spmv(M->u_rows, M->vf, s, M->hilo && M->v64 ? M->vf_lo : nullptr);
+    k_combine_rows<double, TV, kThreads><<<g, kThreads, 0, s>>>(
+        M->u_rows.partial, M->u_rows.n_slabs, ctx->m_k, ctx->D.csr(), v, u, ctx->gc1k, mode,
+        ctx->st, ctx->parts_u);
+  } else {
+    slab_spmv(M->s_rows, ctx->slab_group_f, M->vf, s);
+    k_combine_rows<float, TV, kThreads><<<g, kThreads, 0, s>>>(
+        M->s_rows.partial, M->s_rows.n_slabs, ctx->m_k, ctx->D.csr(), v, u, ctx->gc1k, mode,
+        ctx->st, ctx->parts_u);
   }
-  slab_spmv(M->s_rows, ctx->slab_group_f, M->vf, s);
-  *n_slabs = M->s_rows.n_slabs;
-  return M->s_rows.partial;
 }
-static const float *cols_partials(plsqr_ctx *ctx, cudaStream_t s, int *n_slabs) {
+template <typename TV>
+static void combine_cols(plsqr_ctx *ctx, cudaStream_t s, const TV *u, TV *v, int mode) {
   MixedState *M = ctx->mixed;
   if (M->units) {
-    units_spmv(M->u_cols, M->uf, s);
-    *n_slabs = M->u_cols.n_slabs;
-    return M->u_cols.partial;
+    units_spmv(M->u_cols, M->uf, s, M->hilo && M->v64 ? M->uf_lo : nullptr);
+    k_combine_cols<double, TV, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+        M->u_cols.partial, M->u_cols.n_slabs, ctx->n, ctx->DC.csr(), u, ctx->m_k, v, mode, ctx->st,
+        ctx->parts_v);
+  } else {
+    slab_spmv(M->s_cols, ctx->slab_group_f, M->uf, s);
+    k_combine_cols<float, TV, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
+        M->s_cols.partial, M->s_cols.n_slabs, ctx->n, ctx->DC.csr(), u, ctx->m_k, v, mode, ctx->st,
+        ctx->parts_v);
   }
-  slab_spmv(M->s_cols, ctx->slab_group_f, M->uf, s);
-  *n_slabs = M->s_cols.n_slabs;
-  return M->s_cols.partial;
 }
 
 static void m1f(plsqr_ctx *ctx, cudaStream_t s) {
   MixedState *M = ctx->mixed;
   if (M->slabs) {
-    int ns = 0;
-    const float *pp = rows_partials(ctx, s, &ns);
-    k_combine_rows<float, float, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
-        pp, ns, ctx->m_k, ctx->D.csr(), M->vf, M->uf, ctx->gc1k, kScaleNegAlpha, ctx->st,
-        ctx->parts_u);
+    combine_rows<float>(ctx, s, M->vf, M->uf, kScaleNegAlpha);
     return;
   }
   k_aprod1<float, kThreads, 2><<<ctx->g1k + ctx->g1d, kThreads, 0, s>>>(
@@ -174,10 +202,7 @@ static void m1f(plsqr_ctx *ctx, cudaStream_t s) {
 static void m2f(plsqr_ctx *ctx, cudaStream_t s, int mode) {
   MixedState *M = ctx->mixed;
   if (M->slabs) {
-    int ns = 0;
-    const float *pp = cols_partials(ctx, s, &ns);
-    k_combine_cols<float, float, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
-        pp, ns, ctx->n, ctx->DC.csr(), M->uf, ctx->m_k, M->vf, mode, ctx->st, ctx->parts_v);
+    combine_cols<float>(ctx, s, M->uf, M->vf, mode);
     return;
   }
   k_aprod2<float, kThreads, 2><<<ctx->g2, kThreads, 0, s>>>(
@@ -186,19 +211,13 @@ static void m2f(plsqr_ctx *ctx, cudaStream_t s, int mode) {
 }
 
 // FP64-vector inner sweeps: the products read the FP32 mirrors of v and u
-// (written by the scaling kernels) with the FP32 slab matrix and combine the
-// FP32 partials into the FP64 vectors.
+// (written by the scaling kernels) and combine the partials into the FP64
+// vectors.
 static void m1v(plsqr_ctx *ctx, cudaStream_t s, int mode) {
-  int ns = 0;
-  const float *pp = rows_partials(ctx, s, &ns);
-  k_combine_rows<float, double, kThreads><<<ctx->gc1k + ctx->gc1d, kThreads, 0, s>>>(
-      pp, ns, ctx->m_k, ctx->D.csr(), ctx->v, ctx->u, ctx->gc1k, mode, ctx->st, ctx->parts_u);
+  combine_rows<double>(ctx, s, ctx->v, ctx->u, mode);
 }
 static void m2v(plsqr_ctx *ctx, cudaStream_t s, int mode) {
-  int ns = 0;
-  const float *pp = cols_partials(ctx, s, &ns);
-  k_combine_cols<float, double, kThreads><<<ctx->gc2, kThreads, 0, s>>>(
-      pp, ns, ctx->n, ctx->DC.csr(), ctx->u, ctx->m_k, ctx->v, mode, ctx->st, ctx->parts_v);
+  combine_cols<double>(ctx, s, ctx->u, ctx->v, mode);
 }
 
 static int enqueue_inner64(plsqr_ctx *ctx, cudaStream_t s) {
@@ -207,11 +226,11 @@ static int enqueue_inner64(plsqr_ctx *ctx, cudaStream_t s) {
   const double *xref = ctx->has_ref ? ctx->xref : nullptr;
   m1v(ctx, s, kScaleNegAlpha);
   k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, s>>>(ctx->u, m, ctx->parts_u, ctx->gc1k,
-                                                           ctx->gc1d, ctx->st, 0, M->uf);
+                                                           ctx->gc1d, ctx->st, 0, M->uf, M->uf_lo);
   m2v(ctx, s, kScaleNegBeta);
   k_update_x<kThreads><<<ctx->gvx, kThreads, 0, s>>>(
       ctx->v, ctx->w, M->dx, nullptr, xref, ctx->n, ctx->parts_v, ctx->gc2, ctx->st, ctx->parts_dk,
-      xref ? ctx->parts_err : nullptr, ctx->hist, 0, M->vf, ctx->x);
+      xref ? ctx->parts_err : nullptr, ctx->hist, 0, M->vf, ctx->x, M->vf_lo);
   k_tail<kThreads><<<1, kThreads, 0, s>>>(ctx->st, ctx->parts_dk, xref ? ctx->parts_err : nullptr,
                                            ctx->gvx, ctx->x, ctx->hist);
   CK(cudaGetLastError());
@@ -341,12 +360,12 @@ int mixed_lsqr(plsqr_ctx *ctx, const plsqr_lsqr_args *args, const double *b_k, d
     if (M->v64) {
       // FP64-vector inner solve: scaled r and its FP32 mirror, v = A^T u
       k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(
-          ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d, ctx->st, 1, M->uf);
+          ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d, ctx->st, 1, M->uf, M->uf_lo);
       CK(cudaMemsetAsync(ctx->v, 0, sizeof(double) * ctx->n, ctx->stream));
       m2v(ctx, ctx->stream, kScaleZero);
       k_update_x<kThreads><<<ctx->gvx, kThreads, 0, ctx->stream>>>(
           ctx->v, ctx->w, M->dx, nullptr, nullptr, ctx->n, ctx->parts_v, ctx->gc2, ctx->st,
-          ctx->parts_dk, nullptr, nullptr, 1, M->vf, nullptr);
+          ctx->parts_dk, nullptr, nullptr, 1, M->vf, nullptr, M->vf_lo);
     } else {
       k_norm_u<double, kThreads><<<ctx->gvu, kThreads, 0, ctx->stream>>>(
           ctx->u, m, ctx->parts_u, ctx->g1k, ctx->g1d, ctx->st, 1);

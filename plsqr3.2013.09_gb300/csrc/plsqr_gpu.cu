@@ -274,27 +274,39 @@ template int slab_set_smem<double>(size_t);
 template int slab_set_smem<float>(size_t);
 
 template <typename T>
-void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s) {
+void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s, const T *x_lo) {
   const UnitsArgs<T> A{U.idx,     U.val,     U.slot0,  U.q,     U.c,       U.line,       U.unit_begin,
                        U.n_lines, U.n_slabs, U.slab,   U.n_idx, U.pf_dist, U.pf_pieces};
   cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
+  if constexpr (sizeof(T) == 4) {
+    if (x_lo && U.hilo) {
+      if (U.threads == 512)
+        k_slab_units<T, 512, true><<<U.blocks, 512, U.smem, s>>>(A, U.next, x, x_lo, U.partial);
+      else
+        k_slab_units<T, 1024, true><<<U.blocks, 1024, U.smem, s>>>(A, U.next, x, x_lo, U.partial);
+      return;
+    }
+  }
   if (U.threads == 512)
-    k_slab_units<T, 512><<<U.blocks, 512, U.smem, s>>>(A, U.next, x, U.partial);
+    k_slab_units<T, 512><<<U.blocks, 512, U.smem, s>>>(A, U.next, x, nullptr, U.partial);
   else
-    k_slab_units<T, 1024><<<U.blocks, 1024, U.smem, s>>>(A, U.next, x, U.partial);
+    k_slab_units<T, 1024><<<U.blocks, 1024, U.smem, s>>>(A, U.next, x, nullptr, U.partial);
 }
-template void units_spmv<double>(const DevUnitsT<double> &, const double *, cudaStream_t);
-template void units_spmv<float>(const DevUnitsT<float> &, const float *, cudaStream_t);
+template void units_spmv<double>(const DevUnitsT<double> &, const double *, cudaStream_t,
+                                 const double *);
+template void units_spmv<float>(const DevUnitsT<float> &, const float *, cudaStream_t,
+                                const float *);
 
 template <typename T>
 int units_set_smem(size_t smem) {
   const int bytes = (int)std::max<size_t>(smem, 1);
-  return cudaFuncSetAttribute(k_slab_units<T, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              bytes) ||
-                 cudaFuncSetAttribute(k_slab_units<T, 512>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
-             ? PLSQR_ERR_CUDA
-             : PLSQR_OK;
+  const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  bool bad = cudaFuncSetAttribute(k_slab_units<T, 1024>, attr, bytes) != cudaSuccess ||
+             cudaFuncSetAttribute(k_slab_units<T, 512>, attr, bytes) != cudaSuccess;
+  if constexpr (sizeof(T) == 4)
+    bad = bad || cudaFuncSetAttribute(k_slab_units<T, 1024, true>, attr, bytes) != cudaSuccess ||
+          cudaFuncSetAttribute(k_slab_units<T, 512, true>, attr, bytes) != cudaSuccess;
+  return bad ? PLSQR_ERR_CUDA : PLSQR_OK;
 }
 template int units_set_smem<double>(size_t);
 template int units_set_smem<float>(size_t);

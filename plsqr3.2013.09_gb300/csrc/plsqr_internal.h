@@ -49,10 +49,11 @@ struct DevUnitsT {
   int32_t *q = nullptr, *c = nullptr, *line = nullptr, *unit_begin = nullptr;
   int32_t n_lines = 0, n_slabs = 0, slab = 0, n_idx = 0, n_units = 0;
   int32_t threads = 1024;       // block size of k_slab_units: 1,024 or 512
+  bool hilo = false;            // FP32: shared memory sized for hi + lo pairs
   int32_t pf_dist = 1, pf_pieces = 1;  // L2 prefetch of the unit kernel (set by build_units)
   int64_t slots = 0;
   int *next = nullptr;         // [n_slabs] unit counters, zeroed before every launch
-  T *partial = nullptr;        // [n_slabs * n_lines]
+  double *partial = nullptr;   // [n_slabs * n_lines], FP64 for either value type
   int blocks = 0;
   size_t smem = 0;
 };
@@ -134,15 +135,16 @@ int slab_dyn_blocks(const plsqr_ctx *ctx, bool fp32);
 int slab_plan(plsqr_ctx *ctx);
 template <typename T>
 int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
-                DevUnitsT<T> *out);
+                DevUnitsT<T> *out, bool hilo = false);
 // slabs of `slab` entries over an index space of n_idx: few enough for the
 // build, 16-bit indices, and the slab and summing area of 1,024 threads in
 // shared memory
 template <typename T>
-bool units_fit(int32_t n_idx, int32_t slab);
+bool units_fit(int32_t n_idx, int32_t slab, bool hilo = false);
 // plsqr_gpu.cu: unit product launch and its shared-memory attribute
+// x_lo (FP32 layouts built with hilo): the low halves of the pairs x + x_lo
 template <typename T>
-void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s);
+void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s, const T *x_lo = nullptr);
 template <typename T>
 int units_set_smem(size_t smem);
 // plsqr_gpu.cu: slab product launch and its shared-memory attribute

@@ -138,7 +138,7 @@ template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, 
 // into units of kUnitLines, every unit's groups assigned to 32 lanes.
 template <typename T>
 int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
-                DevUnitsT<T> *out) {
+                DevUnitsT<T> *out, bool hilo) {
   const int n_lines = L.n_lines;
   const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
   if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
@@ -227,11 +227,14 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   dev_free(ctx, d_seg_unit);
   dev_free(ctx, d_seg_pos);
   // PLSQR_UNIT_THREADS=512: two blocks per SM where two slabs fit in shared memory
+  out->hilo = hilo && sizeof(T) == 4;
+  auto smem = [&](int threads) {
+    return out->hilo ? units_smem<T, true>((size_t)std::min(slab, n_idx), threads)
+                     : units_smem<T, false>((size_t)std::min(slab, n_idx), threads);
+  };
   out->threads = 1024;
   if (const char *e = getenv("PLSQR_UNIT_THREADS"))
-    if (atoi(e) == 512 &&
-        2 * (units_smem<T>((size_t)std::min(slab, n_idx), 512) + 1024) <= 228 * 1024)
-      out->threads = 512;
+    if (atoi(e) == 512 && 2 * (smem(512) + 1024) <= 228 * 1024) out->threads = 512;
   out->blocks = ctx->sm_count * (1024 / out->threads);
   // Each lane prefetches all its loads of the next step into L2 (on the
   // 96x96x32 problem against the step after next, first value piece only:
@@ -246,21 +249,22 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
     if (sscanf(e, "%d,%d", &d, &pc) >= 1 && d >= 0 && d <= 16) out->pf_dist = d;
     if (pc >= 1 && pc <= UnitPieces<T>::P) out->pf_pieces = pc;
   }
-  out->smem = units_smem<T>((size_t)std::min(slab, n_idx), out->threads);
+  out->smem = smem(out->threads);
   return PLSQR_OK;
 }
 template int build_units<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
-                                 DevUnitsT<double> *);
+                                 DevUnitsT<double> *, bool);
+template int build_units<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
+                                DevUnitsT<float> *, bool);
 
 template <typename T>
-bool units_fit(int32_t n_idx, int32_t slab) {
-  return slab >= 1 && slab <= 65536 && (n_idx + slab - 1) / slab <= kMaxSlabs &&
-         units_smem<T>((size_t)std::min(slab, n_idx), 1024) <= 227 * 1024;
+bool units_fit(int32_t n_idx, int32_t slab, bool hilo) {
+  const size_t e = (size_t)std::min(slab, n_idx);
+  const size_t smem = hilo && sizeof(T) == 4 ? units_smem<T, true>(e, 1024) : units_smem<T, false>(e, 1024);
+  return slab >= 1 && slab <= 65536 && (n_idx + slab - 1) / slab <= kMaxSlabs && smem <= 227 * 1024;
 }
-template bool units_fit<double>(int32_t, int32_t);
-template bool units_fit<float>(int32_t, int32_t);
-template int build_units<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
-                                DevUnitsT<float> *);
+template bool units_fit<double>(int32_t, int32_t, bool);
+template bool units_fit<float>(int32_t, int32_t, bool);
 
 // Plan the slab paths.  slab_ok: every dimension fits kMaxSlabs slabs of
 // 24,576 FP32 values, so the mixed solver's inner products use FP32 layouts.

@@ -26,6 +26,8 @@
 // persistent blocks, as in k_slab_spmv_dyn.
 #pragma once
 
+#include <type_traits>
+
 #include "slab.cuh"
 
 namespace plsqr {
@@ -82,9 +84,10 @@ __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__r
   }
 }
 
-// partial[s * n_lines + l] = sum over segment (s, l) of val * x_slab[idx].
-// 1,024 threads: one block per SM (the 192 KB slab of x plus the summing
-// area); 512 threads: two blocks per SM on slabs of up to 12,288 entries.
+// partial[s * n_lines + l] = sum over segment (s, l) of val * x_slab[idx],
+// in FP64 for either value type.  1,024 threads: one block per SM (a slab
+// of x of up to 192 KB plus the summing area); 512 threads: two blocks per
+// SM on slabs of half that.
 // Each lane prefetches its loads of a later step into L2 (by default all
 // of the next step's).
 // One step of a lane: its group's 8 values (P coalesced 16-byte loads).
@@ -118,10 +121,15 @@ __device__ __forceinline__ void unit_vals(const float *val, int64_t base, int k,
 // of entries streamed by one lane keeps FP64 accuracy in its sum (a plain
 // FP32 running sum cost the mixed solver 7% more iterations to 1e-6 on the
 // 96x96x32 problem); the FP64 pipe is otherwise idle in the FP32 product.
-template <typename T>
+// FP32 values with the gathered vector as hi + lo FP32 pairs (kHiLo): each
+// product's rounding error recovered by a fused multiply-add, each
+// addition's by the error-free sum of two floats (Knuth), the errors and the
+// lo products summed in a second float: the product of the FP32 values with
+// the FP64 vector to about 2^-44, in FP32 instructions only.
+template <typename T, bool kHiLo = false>
 struct UnitSum;
 template <>
-struct UnitSum<double> {
+struct UnitSum<double, false> {
   double a0 = 0.0, a1 = 0.0;
   __device__ __forceinline__ void add8(const double (&v)[8], const double *xs, uint4 g) {
     a0 = fma(v[0], xs[g.x & 0xffff], a0);
@@ -137,7 +145,7 @@ struct UnitSum<double> {
   __device__ __forceinline__ void reset() { a0 = a1 = 0.0; }
 };
 template <>
-struct UnitSum<float> {
+struct UnitSum<float, false> {
   double a = 0.0;
   __device__ __forceinline__ void add8(const float (&v)[8], const float *xs, uint4 g) {
     float g0 = v[0] * xs[g.x & 0xffff], g1 = v[1] * xs[g.x >> 16];
@@ -152,14 +160,47 @@ struct UnitSum<float> {
   __device__ __forceinline__ double total() const { return a; }
   __device__ __forceinline__ void reset() { a = 0.0; }
 };
+template <>
+struct UnitSum<float, true> {
+  float s = 0.0f, c = 0.0f;  // running sum and its collected errors
+  // rounded intrinsics: no contraction of a product into a later addition
+  __device__ __forceinline__ void add1(float v, float2 x) {
+    const float p = __fmul_rn(v, x.x);
+    const float pe = __fmaf_rn(v, x.x, -p);  // v * x.x - p, exactly
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));  // s + p - t
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(e, __fmaf_rn(v, x.y, pe)));
+  }
+  __device__ __forceinline__ void add8(const float (&v)[8], const float2 *xs, uint4 g) {
+    add1(v[0], xs[g.x & 0xffff]);
+    add1(v[1], xs[g.x >> 16]);
+    add1(v[2], xs[g.y & 0xffff]);
+    add1(v[3], xs[g.y >> 16]);
+    add1(v[4], xs[g.z & 0xffff]);
+    add1(v[5], xs[g.z >> 16]);
+    add1(v[6], xs[g.w & 0xffff]);
+    add1(v[7], xs[g.w >> 16]);
+  }
+  __device__ __forceinline__ double total() const { return (double)s + (double)c; }
+  __device__ __forceinline__ void reset() { s = c = 0.0f; }
+};
 
-template <typename T, int kThreads>
+// The gathered vector's entry type in shared memory.
+template <typename T, bool kHiLo>
+using UnitX = typename std::conditional<kHiLo, float2, T>::type;
+
+// x_lo (kHiLo only): the low halves of the FP32 pairs x + x_lo.
+template <typename T, int kThreads, bool kHiLo = false>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     k_slab_units(UnitsArgs<T> A, int *__restrict__ next, const T *__restrict__ x,
-                 T *__restrict__ partial) {
+                 const T *__restrict__ x_lo, double *__restrict__ partial) {
+  static_assert(!kHiLo || sizeof(T) == 4, "hi + lo pairs are FP32");
+  using X = UnitX<T, kHiLo>;
   constexpr int P = UnitPieces<T>::P;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *xs = reinterpret_cast<T *>(smem_raw);
+  X *xs = reinterpret_cast<X *>(smem_raw);
   // per warp: each lane's first and last line and its FP64 sums for them,
   // after the slab (min(slab, n_idx) entries: the size the launch gives,
   // rounded up to 2 so that the sums after an FP32 slab stay aligned)
@@ -183,9 +224,13 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     if (!left) continue;
     const int64_t xbase = (int64_t)s * A.slab;
     const int len = (int)min((int64_t)A.slab, (int64_t)A.n_idx - xbase);
-    for (int i = threadIdx.x; i < len; i += kThreads) xs[i] = x[xbase + i];
+    if constexpr (kHiLo) {
+      for (int i = threadIdx.x; i < len; i += kThreads) xs[i] = make_float2(x[xbase + i], x_lo[xbase + i]);
+    } else {
+      for (int i = threadIdx.x; i < len; i += kThreads) xs[i] = x[xbase + i];
+    }
     __syncthreads();
-    T *part = partial + (int64_t)s * A.n_lines;
+    double *part = partial + (int64_t)s * A.n_lines;
     for (;;) {
       int u = 0;
       if (lane == 0) u = atomicAdd(next + s, 1);
@@ -205,7 +250,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
         nb = c[li + 1];
       }
       const int li_first = li;
-      UnitSum<T> acc;
+      UnitSum<T, kHiLo> acc;
       double p_first = 0.0, p_last = 0.0;
       int li_last = kUnitLines;
       for (int k = 0; k < q; ++k) {
@@ -213,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
         if (t == nb && t < G) {  // this lane's run enters the next line
           const double a = acc.total();
           if (li == li_first) p_first = a;
-          else part[ln[li]] = (T)a;  // a line wholly inside the run
+          else part[ln[li]] = a;  // a line wholly inside the run
           acc.reset();
           ++li;
           while (c[li + 1] <= t) ++li;
@@ -256,7 +301,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
           if (a != b || lf[a] == lane || ll[a] == lane) {
             double t = lf[a] == lane ? pf[a] : pl[a];
             for (int j = a + 1; j <= b; ++j) t += lf[j] == lane ? pf[j] : pl[j];
-            part[l] = (T)t;
+            part[l] = t;
           }
         }
       }
@@ -268,9 +313,9 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
 
 // Shared memory of k_slab_units: the slab plus 2 FP64 sums and 2 line
 // indices per thread.
-template <typename T>
+template <typename T, bool kHiLo = false>
 __host__ __device__ constexpr size_t units_smem(size_t slab_entries, int threads) {
-  return ((slab_entries + 1) & ~size_t(1)) * sizeof(T) +
+  return ((slab_entries + 1) & ~size_t(1)) * sizeof(UnitX<T, kHiLo>) +
          (size_t)threads * (2 * sizeof(double) + 2 * sizeof(int));
 }
 

@@ -56,10 +56,12 @@ def test_fp64_switches_match_reference(env, pkg, problems, monkeypatch):
 
 
 MIXED_CASES = [
-    {},                                                     # FP32 unit layout (default)
-    {"PLSQR_MIXED_F32VEC": "1"},                            # FP32 vectors in the inner sweeps
+    {},                                                     # FP32 units, hi + lo mirrors (default)
+    {"PLSQR_MIXED_F32VEC": "1"},                            # FP32 vectors (no lo halves)
     {"PLSQR_UNIT_SIZE_F": "1024"},                          # many slabs, short segments
-    {"PLSQR_UNIT_SIZE_F": "24576", "PLSQR_UNIT_THREADS": "512"},  # two blocks per SM
+    {"PLSQR_UNIT_SIZE_F": "12288", "PLSQR_UNIT_THREADS": "512"},  # two blocks per SM
+    {"PLSQR_MIXED_HILO": "0"},                              # the FP32 mirror alone
+    {"PLSQR_MIXED_HILO": "0", "PLSQR_UNIT_SIZE_F": "24576", "PLSQR_UNIT_THREADS": "512"},
     {"PLSQR_MIXED_UNITS": "0"},                             # FP32 slab kernels
     {"PLSQR_MIXED_UNITS": "0", "PLSQR_MIXED_F32VEC": "1"},
     {"PLSQR_MIXED_UNITS": "0", "PLSQR_SLAB_SIZE_F": "1024"},
