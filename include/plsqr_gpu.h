@@ -383,6 +383,15 @@ int plsqr_multi_plan(const plsqr_multi *mp, int32_t *group, int32_t *group_block
  * bit (twice the FP64 instructions); 0 (default): fused multiply-adds in the
  * same order. */
 int plsqr_multi_set_exact(plsqr_multi *mp, int32_t exact);
+/* sweeps > 0: FP32 inner / FP64 outer.  Every problem runs `sweeps`
+ * refinement sweeps; each is an LSQR of lsqr_iteration iterations for the
+ * correction dx on the FP64 residual r = b - A x, with the kernel products
+ * in FP32 values (rounded to nearest) times hi + lo FP32 pairs of the FP64
+ * vectors (error-free FP32 products and sums), vectors, damping products,
+ * norms and recurrence in FP64; x += dx after each sweep.  hist and res then
+ * hold the last sweep's LSQR.  0 (default): one FP64 LSQR.  Not with
+ * exact products (PLSQR_ERR_ARG). */
+int plsqr_multi_set_mixed(plsqr_multi *mp, int32_t sweeps);
 /* Set the barrier wait limit (nanoseconds, >= 1000); default one second. */
 int plsqr_multi_set_wait(plsqr_multi *mp, int64_t wait_ns);
 /* Solve all problems.  x: the solutions one after another (sum of n_p

@@ -151,6 +151,7 @@ SIGNATURES = {
     "plsqr_multi_plan_host": (C.c_int, [vp, vp, i32, i32, f64, vp, vp, C.POINTER(i32)]),
     "plsqr_multi_set_wait": (C.c_int, [vp, i64]),
     "plsqr_multi_set_exact": (C.c_int, [vp, i32]),
+    "plsqr_multi_set_mixed": (C.c_int, [vp, i32]),
     "plsqr_multi_solve": (C.c_int, [vp, vp, vp, vp]),
     "plsqr_multi_check_wait": (C.c_int, [vp, i64]),
     "plsqr_io_read_kernel_info": (C.c_int, [C.c_char_p, i32, vp, vp, C.POINTER(i64)]),

@@ -71,6 +71,11 @@ struct MultiProb {
   const int32_t *cpart;  // [nw + 1] column range of each warp of the group
   const double *b;
   double *u, *v, *w, *x;
+  // mixed precision (plsqr_multi_set_mixed): FP32 kernel values by row and
+  // by column, hi + lo FP32 mirrors of u_k and v, the sweep's correction
+  const float *kr_val32, *kc_val32;
+  float *uh, *ul, *vh, *vl;
+  double *dx;
   plsqr_iter *hist;  // [iters + 1]
   int32_t m_k, m_d, n, iters, itnlim, pad;
   double damp, atol, btol, ctol;
@@ -182,6 +187,37 @@ __device__ __forceinline__ double seq_line(const int32_t *__restrict__ idx,
   return t;
 }
 
+// One line of FP32 values times an FP32 pair vector (xh + xl) by one thread,
+// in stored order: the product's error recovered by a fused multiply-add,
+// the sum's by Knuth's two-sum, both collected with the lo products in a
+// second float; the FP32 values times the FP64 vector to about 2^-44, in
+// FP32 instructions (the FP64 pipe, which bounds the FP64 products of these
+// small problems, stays free).
+__device__ __forceinline__ double seq_line32(const int32_t *__restrict__ idx,
+                                             const float *__restrict__ val, const float *xh,
+                                             const float *xl, int64_t beg, int64_t end) {
+  float s = 0.0f, c = 0.0f;
+  for (int64_t e = beg; e < end; ++e) {
+    const int j = __ldg(idx + e);
+    const float a = __ldg(val + e), h = __ldcg(xh + j), l = __ldcg(xl + j);
+    const float p = __fmul_rn(a, h);
+    const float pe = __fmaf_rn(a, h, -p);
+    const float t = __fadd_rn(s, p);
+    const float bp = __fsub_rn(t, s);
+    const float er = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(er, __fmaf_rn(a, l, pe)));
+  }
+  return (double)s + (double)c;
+}
+
+// FP64 value -> hi + lo FP32 pair
+__device__ __forceinline__ void split_store(float *hi, float *lo, int64_t i, double y) {
+  const float h = (float)y;
+  hi[i] = h;
+  lo[i] = (float)(y - (double)h);
+}
+
 template <bool kExact>
 __device__ __forceinline__ double kernel_row(const MultiProb &P, const double *v, int r) {
   return seq_line<kExact>(P.kr_idx, P.kr_val, v, P.kr_ptr[r], P.kr_ptr[r + 1]);
@@ -207,19 +243,30 @@ struct BlockScalars {
 };
 
 // One problem, by all blocks of the group.  Returns false when the launch is
-// being abandoned (a wait gave up).
-template <bool kExact>
+// being abandoned (a wait gave up).  kMixed: `sweeps` refinement sweeps, each
+// an LSQR of P.iters iterations for the correction dx on the FP64 residual
+// r = b - A x (kernel rows in FP64), with the kernel products in FP32 over
+// hi + lo mirrors of u_k and v; x += dx after each sweep.  The history and
+// the returned state are the last sweep's.
+template <bool kExact, bool kMixed>
 __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double *parts_v,
-                          double *parts_dk, DevState *out, BlockScalars &sh, double *red) {
+                          double *parts_dk, DevState *out, BlockScalars &sh, double *red,
+                          int sweeps) {
   const int tid = threadIdx.x, lane = tid & 31;
   const int gw = g.rank * kMW + (tid >> 5);               // warp of the group
   const int64_t gt = (int64_t)g.rank * kMT + tid;          // thread of the group
   const int64_t gstride = (int64_t)g.nb * kMT;
   const int64_t m = (int64_t)P.m_k + P.m_d;
-  double *u = P.u, *v = P.v, *w = P.w, *x = P.x;
+  double *u = P.u, *v = P.v, *w = P.w;
+  double *x = kMixed ? P.dx : P.x;  // the iterate the LSQR updates
   const bool lead = g.rank == 0;
+  if (!kMixed) sweeps = 1;
+  if (kMixed) {
+    for (int64_t i = gt; i < P.n; i += gstride) P.x[i] = 0.0;
+  }
 
-  // ---- start-up: u = b, v = 0, x = 0 (source/lsqr.c:311-312, 343-409) ----
+  for (int sweep = 0; sweep < sweeps; ++sweep) {
+  // ---- start-up: u = b (kMixed: b - A x), v = 0, x = 0 (source/lsqr.c:311-312, 343-409) ----
   if (tid == 0) {
     DevState &S = sh.S;
     memset(&S, 0, sizeof(S));
@@ -231,10 +278,25 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     S.cs2 = -1.0;
   }
   double sq = 0.0;
-  for (int64_t i = gt; i < m; i += gstride) {
-    const double y = i < P.m_k ? __ldg(P.b + i) : 0.0;
-    u[i] = y;
-    sq = fma(y, y, sq);
+  if (kMixed && sweep > 0) {
+    // FP64 residual of the current x: kernel rows by warp range, damping rows by thread
+    for (int i = P.kpart[gw] + lane; i < P.kpart[gw + 1]; i += 32) {
+      const int r = P.korder[i];
+      const double y = __ldg(P.b + r) - kernel_row<false>(P, P.x, r);
+      u[r] = y;
+      sq = fma(y, y, sq);
+    }
+    for (int64_t r = gt; r < P.m_d; r += gstride) {
+      const double y = -seq_line<false>(P.dr_idx, P.dr_val, P.x, P.dr_ptr[r], P.dr_ptr[r + 1]);
+      u[P.m_k + r] = y;
+      sq = fma(y, y, sq);
+    }
+  } else {
+    for (int64_t i = gt; i < m; i += gstride) {
+      const double y = i < P.m_k ? __ldg(P.b + i) : 0.0;
+      u[i] = y;
+      sq = fma(y, y, sq);
+    }
   }
   for (int64_t i = gt; i < P.n; i += gstride) {
     v[i] = 0.0;
@@ -253,13 +315,19 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
   }
   __syncthreads();
   if (sh.rb != 0.0)
-    for (int64_t i = gt; i < m; i += gstride) u[i] = plsqr::dmul(ld(u + i), sh.rb);
+    for (int64_t i = gt; i < m; i += gstride) {
+      const double y = plsqr::dmul(ld(u + i), sh.rb);
+      u[i] = y;
+      if (kMixed && i < P.m_k) split_store(P.uh, P.ul, i, y);
+    }
   if (!group_sync(g)) return false;
   // v = A^T u (when beta > 0)
   sq = 0.0;
   if (sh.S.s_beta_pos) {
     for (int c = P.cpart[gw] + lane; c < P.cpart[gw + 1]; c += 32) {
-      const double t = plsqr::dadd(kernel_col<kExact>(P, u, c), damp_col<kExact>(P, u, c));  // x += (s_k + s_d)
+      const double k = kMixed ? seq_line32(P.kc_idx, P.kc_val32, P.uh, P.ul, P.kc_ptr[c], P.kc_ptr[c + 1])
+                              : kernel_col<kExact>(P, u, c);
+      const double t = plsqr::dadd(k, damp_col<kExact>(P, u, c));  // x += (s_k + s_d)
       v[c] = t;
       sq = fma(t, t, sq);
     }
@@ -297,6 +365,7 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     double vi = ld(v + i);
     if (sh.ra != 0.0) vi = plsqr::dmul(vi, sh.ra);
     v[i] = vi;
+    if (kMixed) split_store(P.vh, P.vl, i, vi);
     w[i] = sh.ra != 0.0 ? vi : 0.0;
   }
   if (!group_sync(g)) return false;
@@ -305,7 +374,8 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
   // Default mode: u is kept unscaled between B and the next A, so B needs no
   // pass over u and no barrier of its own: C multiplies its column sums by
   // 1/beta and A scales each u element as it reads it (the same product the
-  // reference's scaling rounds).  rb_u: the scale u still carries.
+  // reference's scaling rounds).  rb_u: the scale u still carries.  The
+  // mixed products read the mirror of the unscaled u_k that A writes.
   double rb_u = 1.0;
   for (int it = 0; it < iters; ++it) {
     // A: u = -alpha u + A v
@@ -314,8 +384,11 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     for (int i = P.kpart[gw] + lane; i < P.kpart[gw + 1]; i += 32) {
       const int r = P.korder[i];
       const double ur = kExact ? ld(u + r) : plsqr::dmul(ld(u + r), rb_u);
-      const double y = plsqr::dadd(plsqr::dmul(s1, ur), kernel_row<kExact>(P, v, r));
+      const double k = kMixed ? seq_line32(P.kr_idx, P.kr_val32, P.vh, P.vl, P.kr_ptr[r], P.kr_ptr[r + 1])
+                              : kernel_row<kExact>(P, v, r);
+      const double y = plsqr::dadd(plsqr::dmul(s1, ur), k);
       u[r] = y;
+      if (kMixed) split_store(P.uh, P.ul, r, y);
       sq = fma(y, y, sq);
     }
     for (int64_t r = gt; r < P.m_d; r += gstride) {
@@ -355,7 +428,9 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
       const double s2 = -sh.S.beta;
       const double rb = sh.rb;
       for (int c = P.cpart[gw] + lane; c < P.cpart[gw + 1]; c += 32) {
-        double t = plsqr::dadd(kernel_col<kExact>(P, u, c), damp_col<kExact>(P, u, c));
+        const double k = kMixed ? seq_line32(P.kc_idx, P.kc_val32, P.uh, P.ul, P.kc_ptr[c], P.kc_ptr[c + 1])
+                                : kernel_col<kExact>(P, u, c);
+        double t = plsqr::dadd(k, damp_col<kExact>(P, u, c));
         if (!kExact) t = plsqr::dmul(t, rb);
         const double y = plsqr::dadd(plsqr::dmul(s2, ld(v + c)), t);
         v[c] = y;
@@ -390,6 +465,7 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
         vi = plsqr::dmul(vi, ra);
         v[i] = vi;
       }
+      if (kMixed) split_store(P.vh, P.vl, i, vi);
       const double t = w[i];
       x[i] = plsqr::dadd(plsqr::dmul(t1, t), x[i]);
       w[i] = plsqr::dadd(plsqr::dmul(t2, t), vi);
@@ -403,16 +479,22 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     if (tid == 0) lsqr_tail(sh.S, bs, 0.0, ld(x), lead ? P.hist : nullptr);
     __syncthreads();
   }
+  if (kMixed) {  // x += dx
+    for (int64_t i = gt; i < P.n; i += gstride) P.x[i] = P.x[i] + ld(x + i);
+    if (!group_sync(g)) return false;
+  }
+  }  // sweeps
   if (tid == 0 && lead) *out = sh.S;
   return true;
 }
 
 // The persistent kernel: block b runs the queue of its group.
-template <bool kExact>
+template <bool kExact, bool kMixed>
 __global__ void __launch_bounds__(kMT, 4)  // 4 blocks per SM (64 registers)
     k_multi_lsqr(const MultiProb *__restrict__ probs, const MultiGroup *__restrict__ groups,
                  const int32_t *__restrict__ queue, const int32_t *__restrict__ block_group,
-                 unsigned int *bars, double *parts, DevState *out, int *err, long long wait_ns) {
+                 unsigned int *bars, double *parts, DevState *out, int *err, long long wait_ns,
+                 int sweeps) {
   __shared__ BlockScalars sh;
   __shared__ double red[kMW];
   const int gi = block_group[blockIdx.x];
@@ -421,7 +503,9 @@ __global__ void __launch_bounds__(kMT, 4)  // 4 blocks per SM (64 registers)
   const int nblk = gridDim.x;
   for (int q = G.q_begin; q < G.q_end; ++q) {
     const int p = queue[q];
-    if (!solve_one<kExact>(probs[p], g, parts, parts + nblk, parts + 2 * nblk, out + p, sh, red)) return;
+    if (!solve_one<kExact, kMixed>(probs[p], g, parts, parts + nblk, parts + 2 * nblk, out + p,
+                                   sh, red, sweeps))
+      return;
   }
 }
 
@@ -457,6 +541,7 @@ struct plsqr_multi {
   int64_t device_bytes = 0;
   long long wait_ns = 1000000000LL;
   int exact = 0;  // products in the reference's rounding (DMUL + DADD)
+  int sweeps = 0;  // > 0: FP32-inner / FP64-outer sweeps (plsqr_multi_set_mixed)
   double seconds = 0.0;
   char last_error[512] = {0};
 };
@@ -630,9 +715,11 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
   }
   int occ = 0;
   int occ2 = 0;
-  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_multi_lsqr<false>, kMT, 0));
-  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_multi_lsqr<true>, kMT, 0));
-  occ = std::min(occ, occ2);
+  int occ3 = 0;
+  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_multi_lsqr<false, false>, kMT, 0));
+  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k_multi_lsqr<true, false>, kMT, 0));
+  MK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ3, k_multi_lsqr<false, true>, kMT, 0));
+  occ = std::min({occ, occ2, occ3});
   mp->blocks_per_sm = std::max(1, std::min(occ, 4));
   mp->blocks = mp->sm_count * mp->blocks_per_sm;
   // host copies: pointers as int64, K by row
@@ -722,7 +809,11 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
     const int64_t m = (int64_t)m_k + m_d;
     int64_t *kr_ptr, *kc_ptr, *dr_ptr, *dc_ptr;
     int32_t *kr_idx, *kc_idx, *dr_idx, *dc_idx, *kpart, *cpart, *korder;
-    double *kr_val, *kc_val, *dr_val, *dc_val, *b, *u, *v, *w, *x;
+    double *kr_val, *kc_val, *dr_val, *dc_val, *b, *u, *v, *w, *x, *dx;
+    float *kr_val32, *kc_val32, *uh, *ul, *vh, *vl;
+    // FP32 values of the mixed-precision sweeps, rounded to nearest
+    std::vector<float> krf(krv[(size_t)p].begin(), krv[(size_t)p].end());
+    std::vector<float> kcf(q.k_csc.val, q.k_csc.val + q.k_csc.nnz);
     if ((rc = upload(mp, &kr_ptr, kr[(size_t)p].data(), kr[(size_t)p].size())) ||
         (rc = upload(mp, &kr_idx, kri[(size_t)p].data(), kri[(size_t)p].size())) ||
         (rc = upload(mp, &kr_val, krv[(size_t)p].data(), krv[(size_t)p].size())) ||
@@ -742,7 +833,14 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
         (rc = upload<double>(mp, &u, nullptr, (size_t)m)) ||
         (rc = upload<double>(mp, &v, nullptr, (size_t)n)) ||
         (rc = upload<double>(mp, &w, nullptr, (size_t)n)) ||
-        (rc = upload<double>(mp, &x, nullptr, (size_t)n)))
+        (rc = upload<double>(mp, &x, nullptr, (size_t)n)) ||
+        (rc = upload<double>(mp, &dx, nullptr, (size_t)n)) ||
+        (rc = upload(mp, &kr_val32, krf.data(), krf.size())) ||
+        (rc = upload(mp, &kc_val32, kcf.data(), kcf.size())) ||
+        (rc = upload<float>(mp, &uh, nullptr, (size_t)m_k)) ||
+        (rc = upload<float>(mp, &ul, nullptr, (size_t)m_k)) ||
+        (rc = upload<float>(mp, &vh, nullptr, (size_t)n)) ||
+        (rc = upload<float>(mp, &vl, nullptr, (size_t)n)))
       return rc;
     d.kr_ptr = kr_ptr, d.kr_idx = kr_idx, d.kr_val = kr_val;
     d.kc_ptr = kc_ptr, d.kc_idx = kc_idx, d.kc_val = kc_val;
@@ -750,6 +848,8 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
     d.dc_ptr = dc_ptr, d.dc_idx = dc_idx, d.dc_val = dc_val;
     d.korder = korder, d.kpart = kpart, d.cpart = cpart;
     d.b = b, d.u = u, d.v = v, d.w = w, d.x = x;
+    d.kr_val32 = kr_val32, d.kc_val32 = kc_val32, d.uh = uh, d.ul = ul, d.vh = vh, d.vl = vl;
+    d.dx = dx;
     d.m_k = m_k, d.m_d = m_d, d.n = n, d.iters = q.lsqr_iteration, d.itnlim = q.itnlim;
     d.damp = q.damp, d.atol = q.atol, d.btol = q.btol;
     d.ctol = q.conlim > 0.0 ? 1.0 / q.conlim : 0.0;
@@ -831,7 +931,21 @@ extern "C" int plsqr_multi_set_wait(plsqr_multi *mp, int64_t wait_ns) {
 
 extern "C" int plsqr_multi_set_exact(plsqr_multi *mp, int32_t exact) {
   if (!mp || (exact != 0 && exact != 1)) return PLSQR_ERR_ARG;
+  if (exact && mp->sweeps) {
+    set_error(mp, "exact products are FP64: turn mixed precision off first");
+    return PLSQR_ERR_ARG;
+  }
   mp->exact = exact;
+  return PLSQR_OK;
+}
+
+extern "C" int plsqr_multi_set_mixed(plsqr_multi *mp, int32_t sweeps) {
+  if (!mp || sweeps < 0 || sweeps > 64) return PLSQR_ERR_ARG;
+  if (sweeps && mp->exact) {
+    set_error(mp, "mixed precision needs the default (non-exact) products");
+    return PLSQR_ERR_ARG;
+  }
+  mp->sweeps = sweeps;
   return PLSQR_OK;
 }
 
@@ -844,14 +958,15 @@ extern "C" int plsqr_multi_solve(plsqr_multi *mp, double *x, plsqr_iter *hist,
   MK(cudaMemsetAsync(mp->d_err, 0, sizeof(int), s));
   MK(cudaMemsetAsync(mp->d_hist, 0, sizeof(plsqr_iter) * mp->hist_total, s));
   long long wait = mp->wait_ns;
+  int sweeps = mp->sweeps;
   void *args[] = {&mp->d_probs, &mp->d_groups, &mp->d_queue, &mp->d_block_group,
                   &mp->d_bars,  &mp->d_parts,  &mp->d_out,   &mp->d_err,
-                  &wait};
+                  &wait,        &sweeps};
+  const void *kern = sweeps      ? (const void *)k_multi_lsqr<false, true>
+                     : mp->exact ? (const void *)k_multi_lsqr<true, false>
+                                 : (const void *)k_multi_lsqr<false, false>;
   MK(cudaEventRecord(mp->ev0, s));
-  MK(cudaLaunchCooperativeKernel(mp->exact ? (const void *)k_multi_lsqr<true>
-                                           : (const void *)k_multi_lsqr<false>,
-                                 dim3(mp->blocks), dim3(kMT), args,
-                                 0, s));
+  MK(cudaLaunchCooperativeKernel(kern, dim3(mp->blocks), dim3(kMT), args, 0, s));
   MK(cudaEventRecord(mp->ev1, s));
   MK(cudaEventSynchronize(mp->ev1));
   float ms = 0.f;

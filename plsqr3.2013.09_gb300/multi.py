@@ -113,6 +113,11 @@ class Multi:
         self._check(N.lib().plsqr_multi_set_exact(self._h, int(bool(exact))),
                     "plsqr_multi_set_exact")
 
+    def set_mixed(self, sweeps: int) -> None:
+        """sweeps > 0: FP32 inner / FP64 outer, `sweeps` refinement sweeps of
+        each problem's iteration count; 0: one FP64 LSQR."""
+        self._check(N.lib().plsqr_multi_set_mixed(self._h, int(sweeps)), "plsqr_multi_set_mixed")
+
     def set_wait(self, wait_ns: int) -> None:
         self._check(N.lib().plsqr_multi_set_wait(self._h, int(wait_ns)), "plsqr_multi_set_wait")
 

@@ -109,3 +109,23 @@ def test_damped_problems_match_one_problem_path(pkg, uneven):
             ref = c.lsqr(lsqr_iteration=p.iterations, damp=0.05)
         assert rel(x, ref["x"]) <= 1e-10
         assert np.allclose(h["rnorm"], ref["hist"]["rnorm"], rtol=1e-10, atol=0)
+
+
+def test_mixed_sweeps_reach_fp64_solutions(pkg, uneven):
+    """FP32 inner / FP64 outer (plsqr_multi_set_mixed): every problem within
+    1e-6 of its converged FP64 solution after three sweeps; exact products
+    are refused with it, and the FP64 launch afterwards gives the same bits."""
+    with pkg.multi.Multi(uneven) as mp:
+        base = mp.solve()
+        mp.set_mixed(3)
+        mixed = mp.solve()
+        with pytest.raises(pkg._native.PlsqrError):
+            mp.set_exact(True)
+        mp.set_mixed(0)
+        again = mp.solve()
+    for p, xm, x0, x1, r in zip(uneven, mixed["x"], base["x"], again["x"], mixed["results"]):
+        assert np.array_equal(x0, x1)
+        assert r["itn"] == p.iterations  # the last sweep's LSQR
+        with pkg.Context(p) as c:
+            xs = c.lsqr(lsqr_iteration=600)["x"]
+        assert rel(xm, xs) <= 1e-6, rel(xm, xs)
