@@ -497,7 +497,7 @@ def time_to_tol(pkg, prob, ctx64, iters, tol) -> dict:
 
 
 def warm_time_to_tol(pkg, prob, ctx64, iters, tol, n_train, epochs, n_eval, device) -> dict:
-    """The spec form: learned warm start + mixed precision, against
+    """The target form: learned warm start + mixed precision, against
     plain FP64 LSQR and cold mixed precision, time to `tol` relative error vs
     each instance's FP64 solution (FP64 LSQR run to twice the iterations).
 

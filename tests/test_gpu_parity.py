@@ -2,7 +2,7 @@
 
 Tolerances: the FP64 path must reproduce the reference's x and the
 per-iteration alpha, beta, rnorm, arnorm within 1e-10 relative (the
-spec bar); a single aprod must match the oracle within 1e-12 of
+parity bar of the FP64 path); a single aprod must match the oracle within 1e-12 of
 (|A| |x| + |y|) per element (the GPU sums a row in a different order)."""
 from __future__ import annotations
 
