@@ -159,17 +159,22 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   std::vector<int64_t> uslot;
   int64_t slots = 0;
   std::vector<int32_t> ord((size_t)n_lines);
+  // lines per unit: kUnitLines, or fewer (PLSQR_UNIT_LINES; the unit's other
+  // line slots stay empty) for shorter units and a shorter launch tail
+  int lpu = kUnitLines;
+  if (const char *e = getenv("PLSQR_UNIT_LINES"))
+    if (atoi(e) >= 1 && atoi(e) <= kUnitLines) lpu = atoi(e);
   for (int s = 0; s < n_slabs; ++s) {
     const int64_t *cs = hc.data() + (size_t)s * n_lines;
     for (int l = 0; l < n_lines; ++l) ord[(size_t)l] = l;
     std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return cs[a] > cs[b]; });
     ubeg[(size_t)s] = (int32_t)uq.size();
-    for (int i0 = 0; i0 < n_lines; i0 += kUnitLines) {
+    for (int i0 = 0; i0 < n_lines; i0 += lpu) {
       const int u = (int)uq.size();
       int64_t run = 0;
       for (int i = 0; i < kUnitLines; ++i) {
         uc.push_back((int32_t)run);
-        if (i0 + i < n_lines) {
+        if (i < lpu && i0 + i < n_lines) {
           const int l = ord[(size_t)i0 + i];
           uline.push_back(l);
           seg_unit[(size_t)s * n_lines + l] = u;
