@@ -287,6 +287,16 @@ void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s, const T *x_lo
       return;
     }
   }
+  if constexpr (sizeof(T) == 8) {
+    if (U.chains == 4) {
+      if (U.threads == 512)
+        k_slab_units<T, 512, false, 4><<<U.blocks, 512, U.smem, s>>>(A, U.next, x, nullptr, U.partial);
+      else
+        k_slab_units<T, 1024, false, 4><<<U.blocks, 1024, U.smem, s>>>(A, U.next, x, nullptr,
+                                                                       U.partial);
+      return;
+    }
+  }
   if (U.threads == 512)
     k_slab_units<T, 512><<<U.blocks, 512, U.smem, s>>>(A, U.next, x, nullptr, U.partial);
   else
@@ -306,6 +316,9 @@ int units_set_smem(size_t smem) {
   if constexpr (sizeof(T) == 4)
     bad = bad || cudaFuncSetAttribute(k_slab_units<T, 1024, true>, attr, bytes) != cudaSuccess ||
           cudaFuncSetAttribute(k_slab_units<T, 512, true>, attr, bytes) != cudaSuccess;
+  else
+    bad = bad || cudaFuncSetAttribute(k_slab_units<T, 1024, false, 4>, attr, bytes) != cudaSuccess ||
+          cudaFuncSetAttribute(k_slab_units<T, 512, false, 4>, attr, bytes) != cudaSuccess;
   return bad ? PLSQR_ERR_CUDA : PLSQR_OK;
 }
 template int units_set_smem<double>(size_t);

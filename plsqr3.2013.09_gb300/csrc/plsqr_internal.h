@@ -50,6 +50,7 @@ struct DevUnitsT {
   int32_t n_lines = 0, n_slabs = 0, slab = 0, n_idx = 0, n_units = 0;
   int32_t threads = 1024;       // block size of k_slab_units: 1,024 or 512
   bool hilo = false;            // FP32: shared memory sized for hi + lo pairs
+  int32_t chains = 2;           // FP64: accumulator chains per lane (2 or 4)
   int32_t pf_dist = 1, pf_pieces = 1;  // L2 prefetch of the unit kernel (set by build_units)
   int64_t slots = 0;
   int *next = nullptr;         // [n_slabs] unit counters, zeroed before every launch

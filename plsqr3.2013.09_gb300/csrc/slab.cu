@@ -228,6 +228,15 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   k_units_fill<<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, L.val, n_lines, n_slabs, slab, d_seg_unit,
                                            d_seg_pos, U, out->idx, out->val);
   CK(cudaGetLastError());
+  // PLSQR_UNIT_BANKS=1: order the entries of every step for distinct banks
+  if (const char *e = getenv("PLSQR_UNIT_BANKS"))
+    if (atoi(e) == 1) {
+      const int wave = (sizeof(T) == 8 || hilo) ? 16 : 32;
+      const int nu = (int)uq.size();
+      k_units_banks<<<std::max(1, (nu + 127) / 128), 128, 0, ctx->stream>>>(U, nu, wave, out->idx,
+                                                                           out->val);
+      CK(cudaGetLastError());
+    }
   CK(cudaStreamSynchronize(ctx->stream));
   dev_free(ctx, d_seg_unit);
   dev_free(ctx, d_seg_pos);
@@ -241,6 +250,10 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   if (const char *e = getenv("PLSQR_UNIT_THREADS"))
     if (atoi(e) == 512 && 2 * (smem(512) + 1024) <= 228 * 1024) out->threads = 512;
   out->blocks = ctx->sm_count * (1024 / out->threads);
+  // PLSQR_UNIT_CHAINS=4: four FP64 accumulator chains per lane instead of two
+  out->chains = 2;
+  if (const char *e = getenv("PLSQR_UNIT_CHAINS"))
+    if (atoi(e) == 4) out->chains = 4;
   // Each lane prefetches all its loads of the next step into L2 (on the
   // 96x96x32 problem against the step after next, first value piece only:
   // FP64 A x 2.32 -> 2.29 ms, FP32 A x 1.28 -> 1.22 ms; two steps of all

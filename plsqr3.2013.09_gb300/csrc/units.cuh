@@ -90,6 +90,54 @@ __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__r
 // SM on slabs of half that.
 // Each lane prefetches its loads of a later step into L2 (by default all
 // of the next step's).
+// Setup, optional: order each lane's 8 entries of every step so that the
+// lanes one shared-memory wavefront serves (16 for 8-byte entries: FP64, or
+// FP32 hi + lo pairs; 32 for 4-byte ones) gather from distinct banks where
+// they can.  The kernel's e-th gather of a step reads entry e of every
+// lane's group; the entries of a group may come in any order (they are
+// summed into the lane's line either way).  Greedy, one thread per unit:
+// for e = 0..7, lane by lane, the lane's remaining entry whose bank the
+// wavefront has used least so far.
+template <typename T>
+__global__ void k_units_banks(UnitsArgs<T> U, int n_units, int lanes_per_wave,
+                              uint16_t *__restrict__ sidx, T *__restrict__ sval) {
+  constexpr int E = UnitPieces<T>::E, P = UnitPieces<T>::P;
+  const int banks = lanes_per_wave;  // bank groups one entry occupies: 32 / entry words
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n_units; u += gridDim.x * blockDim.x) {
+    const int q = U.q[u];
+    const int64_t base = U.slot0[u];
+    for (int k = 0; k < q; ++k)
+      for (int h = 0; h < 32; h += lanes_per_wave) {
+        uint16_t id[32][8];
+        T v[32][8];
+        unsigned char used[32];
+        for (int j = 0; j < lanes_per_wave; ++j) {
+          used[j] = 0;
+          for (int w = 0; w < 8; ++w) {
+            id[j][w] = sidx[(base + (int64_t)k * 32 + h + j) * 8 + w];
+            v[j][w] = sval[(base * P + ((int64_t)k * P + w / E) * 32 + h + j) * E + w % E];
+          }
+        }
+        for (int e = 0; e < 8; ++e) {
+          int cnt[32];
+          for (int b = 0; b < banks; ++b) cnt[b] = 0;
+          for (int j = 0; j < lanes_per_wave; ++j) {
+            int best = -1, bc = 1 << 30;
+            for (int w = 0; w < 8; ++w)
+              if (!((used[j] >> w) & 1) && cnt[id[j][w] % banks] < bc) {
+                bc = cnt[id[j][w] % banks];
+                best = w;
+              }
+            used[j] |= (unsigned char)(1u << best);
+            ++cnt[id[j][best] % banks];
+            sidx[(base + (int64_t)k * 32 + h + j) * 8 + e] = id[j][best];
+            sval[(base * P + ((int64_t)k * P + e / E) * 32 + h + j) * E + e % E] = v[j][best];
+          }
+        }
+      }
+  }
+}
+
 // One step of a lane: its group's 8 values (P coalesced 16-byte loads).
 __device__ __forceinline__ void unit_vals(const double *val, int64_t base, int k, int lane,
                                           double (&v)[8]) {
@@ -126,10 +174,10 @@ __device__ __forceinline__ void unit_vals(const float *val, int64_t base, int k,
 // addition's by the error-free sum of two floats (Knuth), the errors and the
 // lo products summed in a second float: the product of the FP32 values with
 // the FP64 vector to about 2^-44, in FP32 instructions only.
-template <typename T, bool kHiLo = false>
+template <typename T, bool kHiLo = false, int kChains = 2>
 struct UnitSum;
 template <>
-struct UnitSum<double, false> {
+struct UnitSum<double, false, 2> {
   double a0 = 0.0, a1 = 0.0;
   __device__ __forceinline__ void add8(const double (&v)[8], const double *xs, uint4 g) {
     a0 = fma(v[0], xs[g.x & 0xffff], a0);
@@ -144,8 +192,25 @@ struct UnitSum<double, false> {
   __device__ __forceinline__ double total() const { return a0 + a1; }
   __device__ __forceinline__ void reset() { a0 = a1 = 0.0; }
 };
+// four chains: half the dependent fused multiply-adds per step
 template <>
-struct UnitSum<float, false> {
+struct UnitSum<double, false, 4> {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  __device__ __forceinline__ void add8(const double (&v)[8], const double *xs, uint4 g) {
+    a0 = fma(v[0], xs[g.x & 0xffff], a0);
+    a1 = fma(v[1], xs[g.x >> 16], a1);
+    a2 = fma(v[2], xs[g.y & 0xffff], a2);
+    a3 = fma(v[3], xs[g.y >> 16], a3);
+    a0 = fma(v[4], xs[g.z & 0xffff], a0);
+    a1 = fma(v[5], xs[g.z >> 16], a1);
+    a2 = fma(v[6], xs[g.w & 0xffff], a2);
+    a3 = fma(v[7], xs[g.w >> 16], a3);
+  }
+  __device__ __forceinline__ double total() const { return (a0 + a1) + (a2 + a3); }
+  __device__ __forceinline__ void reset() { a0 = a1 = a2 = a3 = 0.0; }
+};
+template <>
+struct UnitSum<float, false, 2> {
   double a = 0.0;
   __device__ __forceinline__ void add8(const float (&v)[8], const float *xs, uint4 g) {
     float g0 = v[0] * xs[g.x & 0xffff], g1 = v[1] * xs[g.x >> 16];
@@ -161,7 +226,7 @@ struct UnitSum<float, false> {
   __device__ __forceinline__ void reset() { a = 0.0; }
 };
 template <>
-struct UnitSum<float, true> {
+struct UnitSum<float, true, 2> {
   float s = 0.0f, c = 0.0f;  // running sum and its collected errors
   // rounded intrinsics: no contraction of a product into a later addition
   __device__ __forceinline__ void add1(float v, float2 x) {
@@ -192,7 +257,7 @@ template <typename T, bool kHiLo>
 using UnitX = typename std::conditional<kHiLo, float2, T>::type;
 
 // x_lo (kHiLo only): the low halves of the FP32 pairs x + x_lo.
-template <typename T, int kThreads, bool kHiLo = false>
+template <typename T, int kThreads, bool kHiLo = false, int kChains = 2>
 __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
     k_slab_units(UnitsArgs<T> A, int *__restrict__ next, const T *__restrict__ x,
                  const T *__restrict__ x_lo, double *__restrict__ partial) {
@@ -250,7 +315,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
         nb = c[li + 1];
       }
       const int li_first = li;
-      UnitSum<T, kHiLo> acc;
+      UnitSum<T, kHiLo, kChains> acc;
       double p_first = 0.0, p_last = 0.0;
       int li_last = kUnitLines;
       for (int k = 0; k < q; ++k) {

@@ -37,6 +37,9 @@ FP64_CASES = [
     {"PLSQR_SLABS": "2", "PLSQR_UNROLL": "4"},
     {"PLSQR_SLABS": "2", "PLSQR_BLOCKS_PER_SM": "1"},
     {"PLSQR_UNIT_THREADS": "512", "PLSQR_SLAB_SIZE": "12288"},  # two unit blocks per SM
+    {"PLSQR_UNIT_CHAINS": "4"},                              # four accumulator chains
+    {"PLSQR_UNIT_BANKS": "1"},                               # bank-aware entry order
+    {"PLSQR_UNIT_LINES": "8"},                               # short units
     {"PLSQR_NATURAL_ORDER": "1", "PLSQR_SLABS": "0"},
 ]
 
@@ -60,7 +63,9 @@ MIXED_CASES = [
     {"PLSQR_MIXED_F32VEC": "1"},                            # FP32 vectors (no lo halves)
     {"PLSQR_UNIT_SIZE_F": "1024"},                          # many slabs, short segments
     {"PLSQR_UNIT_SIZE_F": "12288", "PLSQR_UNIT_THREADS": "512"},  # two blocks per SM
+    {"PLSQR_UNIT_BANKS": "1"},                              # bank-aware entry order
     {"PLSQR_MIXED_HILO": "0"},                              # the FP32 mirror alone
+    {"PLSQR_MIXED_HILO": "0", "PLSQR_UNIT_BANKS": "1"},
     {"PLSQR_MIXED_HILO": "0", "PLSQR_UNIT_SIZE_F": "24576", "PLSQR_UNIT_THREADS": "512"},
     {"PLSQR_MIXED_UNITS": "0"},                             # FP32 slab kernels
     {"PLSQR_MIXED_UNITS": "0", "PLSQR_MIXED_F32VEC": "1"},
