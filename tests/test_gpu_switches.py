@@ -63,7 +63,7 @@ MIXED_CASES = [
     {"PLSQR_MIXED_F32VEC": "1"},                            # FP32 vectors (no lo halves)
     {"PLSQR_UNIT_SIZE_F": "1024"},                          # many slabs, short segments
     {"PLSQR_UNIT_SIZE_F": "12288", "PLSQR_UNIT_THREADS": "512"},  # two blocks per SM
-    {"PLSQR_UNIT_BANKS": "1"},                              # bank-aware entry order
+    {"PLSQR_UNIT_BANKS": "0"},                              # entries in fill order
     {"PLSQR_MIXED_HILO": "0"},                              # the FP32 mirror alone
     {"PLSQR_MIXED_HILO": "0", "PLSQR_UNIT_BANKS": "1"},
     {"PLSQR_MIXED_HILO": "0", "PLSQR_UNIT_SIZE_F": "24576", "PLSQR_UNIT_THREADS": "512"},
