@@ -74,7 +74,7 @@ struct MultiProb {
   // mixed precision (plsqr_multi_set_mixed): FP32 kernel values by row and
   // by column, hi + lo FP32 mirrors of u_k and v, the sweep's correction
   const float *kr_val32, *kc_val32;
-  float *uh, *ul, *vh, *vl;
+  float2 *uhl, *vhl;  // (hi, lo) pairs: one 8-byte gather per nonzero
   double *dx;
   plsqr_iter *hist;  // [iters + 1]
   int32_t m_k, m_d, n, iters, itnlim, pad;
@@ -187,19 +187,19 @@ __device__ __forceinline__ double seq_line(const int32_t *__restrict__ idx,
   return t;
 }
 
-// One line of FP32 values times an FP32 pair vector (xh + xl) by one thread,
-// in stored order: the product's error recovered by a fused multiply-add,
-// the sum's by Knuth's two-sum, both collected with the lo products in a
-// second float; the FP32 values times the FP64 vector to about 2^-44, in
-// FP32 instructions (the FP64 pipe, which bounds the FP64 products of these
-// small problems, stays free).
+// One line of FP32 values times a vector of (hi, lo) FP32 pairs by one
+// thread, in stored order: the product's error recovered by a fused
+// multiply-add, the sum's by Knuth's two-sum, both collected with the lo
+// products in a second float; the FP32 values times the FP64 vector to
+// about 2^-44, in FP32 instructions only.
 __device__ __forceinline__ double seq_line32(const int32_t *__restrict__ idx,
-                                             const float *__restrict__ val, const float *xh,
-                                             const float *xl, int64_t beg, int64_t end) {
+                                             const float *__restrict__ val, const float2 *xhl,
+                                             int64_t beg, int64_t end) {
   float s = 0.0f, c = 0.0f;
   for (int64_t e = beg; e < end; ++e) {
     const int j = __ldg(idx + e);
-    const float a = __ldg(val + e), h = __ldcg(xh + j), l = __ldcg(xl + j);
+    const float2 x = __ldcg(xhl + j);
+    const float a = __ldg(val + e), h = x.x, l = x.y;
     const float p = __fmul_rn(a, h);
     const float pe = __fmaf_rn(a, h, -p);
     const float t = __fadd_rn(s, p);
@@ -212,10 +212,9 @@ __device__ __forceinline__ double seq_line32(const int32_t *__restrict__ idx,
 }
 
 // FP64 value -> hi + lo FP32 pair
-__device__ __forceinline__ void split_store(float *hi, float *lo, int64_t i, double y) {
+__device__ __forceinline__ void split_store(float2 *hl, int64_t i, double y) {
   const float h = (float)y;
-  hi[i] = h;
-  lo[i] = (float)(y - (double)h);
+  hl[i] = make_float2(h, (float)(y - (double)h));
 }
 
 template <bool kExact>
@@ -318,14 +317,14 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     for (int64_t i = gt; i < m; i += gstride) {
       const double y = plsqr::dmul(ld(u + i), sh.rb);
       u[i] = y;
-      if (kMixed && i < P.m_k) split_store(P.uh, P.ul, i, y);
+      if (kMixed && i < P.m_k) split_store(P.uhl, i, y);
     }
   if (!group_sync(g)) return false;
   // v = A^T u (when beta > 0)
   sq = 0.0;
   if (sh.S.s_beta_pos) {
     for (int c = P.cpart[gw] + lane; c < P.cpart[gw + 1]; c += 32) {
-      const double k = kMixed ? seq_line32(P.kc_idx, P.kc_val32, P.uh, P.ul, P.kc_ptr[c], P.kc_ptr[c + 1])
+      const double k = kMixed ? seq_line32(P.kc_idx, P.kc_val32, P.uhl, P.kc_ptr[c], P.kc_ptr[c + 1])
                               : kernel_col<kExact>(P, u, c);
       const double t = plsqr::dadd(k, damp_col<kExact>(P, u, c));  // x += (s_k + s_d)
       v[c] = t;
@@ -365,7 +364,7 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     double vi = ld(v + i);
     if (sh.ra != 0.0) vi = plsqr::dmul(vi, sh.ra);
     v[i] = vi;
-    if (kMixed) split_store(P.vh, P.vl, i, vi);
+    if (kMixed) split_store(P.vhl, i, vi);
     w[i] = sh.ra != 0.0 ? vi : 0.0;
   }
   if (!group_sync(g)) return false;
@@ -384,11 +383,11 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
     for (int i = P.kpart[gw] + lane; i < P.kpart[gw + 1]; i += 32) {
       const int r = P.korder[i];
       const double ur = kExact ? ld(u + r) : plsqr::dmul(ld(u + r), rb_u);
-      const double k = kMixed ? seq_line32(P.kr_idx, P.kr_val32, P.vh, P.vl, P.kr_ptr[r], P.kr_ptr[r + 1])
+      const double k = kMixed ? seq_line32(P.kr_idx, P.kr_val32, P.vhl, P.kr_ptr[r], P.kr_ptr[r + 1])
                               : kernel_row<kExact>(P, v, r);
       const double y = plsqr::dadd(plsqr::dmul(s1, ur), k);
       u[r] = y;
-      if (kMixed) split_store(P.uh, P.ul, r, y);
+      if (kMixed) split_store(P.uhl, r, y);
       sq = fma(y, y, sq);
     }
     for (int64_t r = gt; r < P.m_d; r += gstride) {
@@ -428,7 +427,7 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
       const double s2 = -sh.S.beta;
       const double rb = sh.rb;
       for (int c = P.cpart[gw] + lane; c < P.cpart[gw + 1]; c += 32) {
-        const double k = kMixed ? seq_line32(P.kc_idx, P.kc_val32, P.uh, P.ul, P.kc_ptr[c], P.kc_ptr[c + 1])
+        const double k = kMixed ? seq_line32(P.kc_idx, P.kc_val32, P.uhl, P.kc_ptr[c], P.kc_ptr[c + 1])
                                 : kernel_col<kExact>(P, u, c);
         double t = plsqr::dadd(k, damp_col<kExact>(P, u, c));
         if (!kExact) t = plsqr::dmul(t, rb);
@@ -465,7 +464,7 @@ __device__ bool solve_one(const MultiProb &P, Group &g, double *parts_u, double 
         vi = plsqr::dmul(vi, ra);
         v[i] = vi;
       }
-      if (kMixed) split_store(P.vh, P.vl, i, vi);
+      if (kMixed) split_store(P.vhl, i, vi);
       const double t = w[i];
       x[i] = plsqr::dadd(plsqr::dmul(t1, t), x[i]);
       w[i] = plsqr::dadd(plsqr::dmul(t2, t), vi);
@@ -810,7 +809,8 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
     int64_t *kr_ptr, *kc_ptr, *dr_ptr, *dc_ptr;
     int32_t *kr_idx, *kc_idx, *dr_idx, *dc_idx, *kpart, *cpart, *korder;
     double *kr_val, *kc_val, *dr_val, *dc_val, *b, *u, *v, *w, *x, *dx;
-    float *kr_val32, *kc_val32, *uh, *ul, *vh, *vl;
+    float *kr_val32, *kc_val32;
+    float2 *uhl, *vhl;
     // FP32 values of the mixed-precision sweeps, rounded to nearest
     std::vector<float> krf(krv[(size_t)p].begin(), krv[(size_t)p].end());
     std::vector<float> kcf(q.k_csc.val, q.k_csc.val + q.k_csc.nnz);
@@ -837,10 +837,8 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
         (rc = upload<double>(mp, &dx, nullptr, (size_t)n)) ||
         (rc = upload(mp, &kr_val32, krf.data(), krf.size())) ||
         (rc = upload(mp, &kc_val32, kcf.data(), kcf.size())) ||
-        (rc = upload<float>(mp, &uh, nullptr, (size_t)m_k)) ||
-        (rc = upload<float>(mp, &ul, nullptr, (size_t)m_k)) ||
-        (rc = upload<float>(mp, &vh, nullptr, (size_t)n)) ||
-        (rc = upload<float>(mp, &vl, nullptr, (size_t)n)))
+        (rc = upload<float2>(mp, &uhl, nullptr, (size_t)m_k)) ||
+        (rc = upload<float2>(mp, &vhl, nullptr, (size_t)n)))
       return rc;
     d.kr_ptr = kr_ptr, d.kr_idx = kr_idx, d.kr_val = kr_val;
     d.kc_ptr = kc_ptr, d.kc_idx = kc_idx, d.kc_val = kc_val;
@@ -848,7 +846,7 @@ static int multi_build(plsqr_multi *mp, const plsqr_problem *probs) {
     d.dc_ptr = dc_ptr, d.dc_idx = dc_idx, d.dc_val = dc_val;
     d.korder = korder, d.kpart = kpart, d.cpart = cpart;
     d.b = b, d.u = u, d.v = v, d.w = w, d.x = x;
-    d.kr_val32 = kr_val32, d.kc_val32 = kc_val32, d.uh = uh, d.ul = ul, d.vh = vh, d.vl = vl;
+    d.kr_val32 = kr_val32, d.kc_val32 = kc_val32, d.uhl = uhl, d.vhl = vhl;
     d.dx = dx;
     d.m_k = m_k, d.m_d = m_d, d.n = n, d.iters = q.lsqr_iteration, d.itnlim = q.itnlim;
     d.damp = q.damp, d.atol = q.atol, d.btol = q.btol;
