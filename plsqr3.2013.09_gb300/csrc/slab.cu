@@ -237,8 +237,8 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   if (banks) {
     const int wave = (sizeof(T) == 8 || hilo) ? 16 : 32;
     const int nu = (int)uq.size();
-    k_units_banks<<<std::max(1, (nu + 127) / 128), 128, 0, ctx->stream>>>(U, nu, wave, out->idx,
-                                                                         out->val);
+    k_units_banks<<<std::max(1, (nu + 3) / 4), 128, 0, ctx->stream>>>(U, nu, wave, out->idx,
+                                                                     out->val);
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(ctx->stream));

@@ -95,18 +95,20 @@ __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__r
 // FP32 hi + lo pairs; 32 for 4-byte ones) gather from distinct banks where
 // they can.  The kernel's e-th gather of a step reads entry e of every
 // lane's group; the entries of a group may come in any order (they are
-// summed into the lane's line either way).  Greedy, one thread per unit:
-// for e = 0..7, lane by lane, the lane's remaining entry whose bank the
-// wavefront has used least so far.
+// summed into the lane's line either way).  Greedy, a warp per unit and a
+// thread per step: for e = 0..7, lane by lane, the lane's remaining entry
+// whose bank the wavefront has used least so far.
 template <typename T>
 __global__ void k_units_banks(UnitsArgs<T> U, int n_units, int lanes_per_wave,
                               uint16_t *__restrict__ sidx, T *__restrict__ sval) {
   constexpr int E = UnitPieces<T>::E, P = UnitPieces<T>::P;
   const int banks = lanes_per_wave;  // bank groups one entry occupies: 32 / entry words
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n_units; u += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n_units; u += warps) {
     const int q = U.q[u];
     const int64_t base = U.slot0[u];
-    for (int k = 0; k < q; ++k)
+    for (int k = lane; k < q; k += 32)
       for (int h = 0; h < 32; h += lanes_per_wave) {
         uint16_t id[32][8];
         T v[32][8];
