@@ -383,10 +383,11 @@ def main() -> int:
                          + f", {s['seconds']:.1f} s"}
     if rank != 0:
         return 0
-    # per solve: start-up (sum of squares, norm, A^T y as slab product +
-    # combine, update) and six kernels per graph-replayed iteration (A x, norm,
-    # slab product, combine, update, tail)
-    launches = (5 + 6 * iters) * args.steps
+    # per solve: start-up (sum of squares, norm, A^T y as unit product +
+    # combine, update) and seven kernels per graph-replayed iteration (A x as
+    # unit product + combine, norm, A^T y as unit product + combine, update,
+    # tail); the ncu launch list of a 20-iteration solve counts 145
+    launches = (5 + 7 * iters) * args.steps
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
