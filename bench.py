@@ -270,6 +270,8 @@ def main() -> int:
                 "cpu_baseline": {"value": value, "unit": UNIT, "cores": per[0]["threads"],
                                  "kind": "port", "cpu_model": cpu_model(),
                                  "seconds_per_iteration": secs / its,
+                                 "loop_seconds": secs,
+                                 "wall_seconds_with_startup": sum(s["wall_seconds"] for s in per),
                                  "sample": cpu_sample_text(args.config, args.cpu_iterations,
                                                            args.steps)},
                 "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -379,6 +381,8 @@ def main() -> int:
         cpu = {"value": bytes_it * s["iterations"] / s["seconds"] / 1e9, "unit": UNIT,
                "cores": s["threads"], "kind": "port", "cpu_model": cpu_model(),
                "seconds_per_iteration": s["seconds"] / s["iterations"],
+               "loop_seconds": s["seconds"],
+               "wall_seconds_with_startup": s["wall_seconds"],
                "sample": cpu_sample_text(args.config, s["iterations"])
                          + f", {s['seconds']:.1f} s"}
     if rank != 0:
