@@ -133,11 +133,16 @@ __global__ void __launch_bounds__(kNrmThreads)
   }
 }
 
+// Terms staged a chunk at a time: the warp loads the next chunk of terms
+// (coalesced, 8 per lane) while lane 0 adds up the current one from shared
+// memory, so the chain of additions no longer waits on a global load.
+constexpr int kChainChunk = 256;
+
 // The ordered sum of one segment's terms on one thread (lane 0 of the
-// segment's warp; the other lanes only help find the scale), terms loaded
-// eight ahead of the chain of additions; source/mycblas.c:182-222:
-// scale * sqrt(ssq), |x[0]| for n = 1, 0 for n < 1.  Valid in lane 0.
-__device__ __forceinline__ double nrm_chain(const NrmArgs &a, const NrmSeg &s) {
+// segment's warp; the other lanes find the scale and stage the terms);
+// source/mycblas.c:182-222: scale * sqrt(ssq), |x[0]| for n = 1, 0 for
+// n < 1.  Valid in lane 0.  buf: 2 * kChainChunk doubles of the warp.
+__device__ __forceinline__ double nrm_chain(const NrmArgs &a, const NrmSeg &s, double *buf) {
   const int lane = threadIdx.x & 31;
   if (s.n <= 0) return 0.0;
   if (s.n == 1) return fabs(s.x[0]);
@@ -145,35 +150,58 @@ __device__ __forceinline__ double nrm_chain(const NrmArgs &a, const NrmSeg &s) {
   for (int b = lane; b < s.nb; b += 32) scale = fmax(scale, a.bmax[s.b0 + b]);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) scale = fmax(scale, __shfl_xor_sync(0xffffffffu, scale, o));
-  if (lane != 0) return 0.0;
+  const int64_t n = s.n;
   double ssq = 1.0;
-  int64_t i0 = 0;
-  for (; i0 + 8 <= s.n; i0 += 8) {
-    double t[8];
-    unsigned neg = 0;  // any new scale among the eight (rare: records of a running maximum)
+  double r[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      t[k] = s.terms[i0 + k];
-      neg |= (unsigned)(__double2hiint(t[k]) >> 31);
-    }
-    // the common case keeps one addition per term on the chain (a select
-    // between the two updates would put both multiplies on it as well)
-    if (!neg) {
+  for (int k = 0; k < 8; ++k) {
+    const int64_t i = k * 32 + lane;
+    r[k] = i < n ? s.terms[i] : 0.0;
+  }
+  for (int64_t c0 = 0; c0 < n; c0 += kChainChunk) {
+    double *bc = buf + ((c0 / kChainChunk) & 1) * kChainChunk;
 #pragma unroll
-      for (int k = 0; k < 8; ++k) ssq = dadd(ssq, t[k]);
-    } else {
+    for (int k = 0; k < 8; ++k) bc[k * 32 + lane] = r[k];
+    __syncwarp();
+    if (c0 + kChainChunk < n) {
+#pragma unroll
       for (int k = 0; k < 8; ++k) {
-        if (signbit(t[k])) ssq = dadd(1.0, dmul(dmul(ssq, -t[k]), -t[k]));
-        else ssq = dadd(ssq, t[k]);
+        const int64_t i = c0 + kChainChunk + k * 32 + lane;
+        r[k] = i < n ? s.terms[i] : 0.0;
       }
     }
+    if (lane == 0) {
+      const int cnt = (int)(n - c0 < kChainChunk ? n - c0 : kChainChunk);
+      int j = 0;
+      for (; j + 8 <= cnt; j += 8) {
+        double t[8];
+        unsigned neg = 0;  // any new scale among the eight (rare: records of a running maximum)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          t[k] = bc[j + k];
+          neg |= (unsigned)(__double2hiint(t[k]) >> 31);
+        }
+        // the common case keeps one addition per term on the chain (a select
+        // between the two updates would put both multiplies on it as well)
+        if (!neg) {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) ssq = dadd(ssq, t[k]);
+        } else {
+          for (int k = 0; k < 8; ++k) {
+            if (signbit(t[k])) ssq = dadd(1.0, dmul(dmul(ssq, -t[k]), -t[k]));
+            else ssq = dadd(ssq, t[k]);
+          }
+        }
+      }
+      for (; j < cnt; ++j) {
+        const double t = bc[j];
+        if (signbit(t)) ssq = dadd(1.0, dmul(dmul(ssq, -t), -t));
+        else ssq = dadd(ssq, t);
+      }
+    }
+    __syncwarp();
   }
-  for (; i0 < s.n; ++i0) {
-    const double t = s.terms[i0];
-    if (signbit(t)) ssq = dadd(1.0, dmul(dmul(ssq, -t), -t));
-    else ssq = dadd(ssq, t);
-  }
-  return dmul(scale, __dsqrt_rn(ssq));
+  return lane == 0 ? dmul(scale, __dsqrt_rn(ssq)) : 0.0;
 }
 
 // Phase 3: one warp per segment (its lane 0 runs the chain), then the norm
@@ -183,9 +211,10 @@ __device__ __forceinline__ double nrm_chain(const NrmArgs &a, const NrmSeg &s) {
 __global__ void __launch_bounds__(64) k_nrm_chain(NrmArgs a, int kind, DevState *__restrict__ st) {
   if (kind == kNrmAlpha && !st->s_beta_pos) return;
   __shared__ double res[2];
+  __shared__ double buf[2][2 * kChainChunk];
   const int w = threadIdx.x >> 5;
   if (w < a.nseg) {
-    const double r = nrm_chain(a, a.seg[w]);
+    const double r = nrm_chain(a, a.seg[w], buf[w]);
     if ((threadIdx.x & 31) == 0) res[w] = r;
   }
   __syncthreads();
@@ -382,22 +411,40 @@ __global__ void __launch_bounds__(32)
                const double *__restrict__ parts_err, int gp, const double *__restrict__ x,
                plsqr_iter *__restrict__ hist) {
   const int lane = threadIdx.x;
+  __shared__ double buf[2 * kChainChunk];
   double e2 = 0.0;
   if (parts_err) {
     for (int b = lane; b < gp; b += 32) e2 += parts_err[b];
     e2 = warp_sum(e2);
   }
-  if (lane != 0) return;
-  double dk = 0.0;  // one thread, terms loaded eight ahead
-  int i0 = 0;
-  for (; i0 + 8 <= n; i0 += 8) {
-    double t[8];
+  // lane 0 adds the terms in element order; the warp stages them (as in
+  // nrm_chain)
+  double dk = 0.0;
+  double r[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) t[k] = dk_terms[i0 + k];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) dk = dadd(t[k], dk);
+  for (int k = 0; k < 8; ++k) {
+    const int i = k * 32 + lane;
+    r[k] = i < n ? dk_terms[i] : 0.0;
   }
-  for (; i0 < n; ++i0) dk = dadd(dk_terms[i0], dk);
+  for (int c0 = 0; c0 < n; c0 += kChainChunk) {
+    double *bc = buf + ((c0 / kChainChunk) & 1) * kChainChunk;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) bc[k * 32 + lane] = r[k];
+    __syncwarp();
+    if (c0 + kChainChunk < n) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int i = c0 + kChainChunk + k * 32 + lane;
+        r[k] = i < n ? dk_terms[i] : 0.0;
+      }
+    }
+    if (lane == 0) {
+      const int cnt = n - c0 < kChainChunk ? n - c0 : kChainChunk;
+      for (int j = 0; j < cnt; ++j) dk = dadd(bc[j], dk);
+    }
+    __syncwarp();
+  }
+  if (lane != 0) return;
   lsqr_tail(*st, dk, e2, x[0], hist);
 }
 
