@@ -1,4 +1,5 @@
-// Unit layout of the kernel matrix, for the FP64 products on slabs.
+// Unit layout of the kernel matrix, for the products on slabs: FP64, and
+// FP32 for the mixed solver's inner sweeps.
 //
 // The slab layout (slab.cuh) hands each line's segment to a group of 8
 // lanes; a segment of ~57 groups of 8 entries then leaves the group's last
