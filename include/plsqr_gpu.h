@@ -175,6 +175,14 @@ typedef struct plsqr_ctx plsqr_ctx;
 /* ---- library ----------------------------------------------------------- */
 const char *plsqr_strerror(int code);
 int plsqr_abi_version(void);
+/* Bounds checks.  *checked = 1 in the bounds-checked build of the library
+ * (compiled with -DPLSQR_CHECK: the unit-layout kernels check every slot,
+ * gather index, line and lane they touch, record a failed check and skip the
+ * access), 0 in the normal build; *flags = the checks that failed on the
+ * current device since the last reset (bits: 1 slot, 2 gather index, 4 line,
+ * 8 lane, 16 fill; always 0 in the normal build).  No counterpart in the
+ * reference. */
+int plsqr_check_flags(int32_t *checked, uint32_t *flags, int32_t reset);
 void plsqr_default_opts(plsqr_opts *opts);
 void plsqr_default_lsqr_args(plsqr_lsqr_args *args);
 /* Number of CUDA devices; 0 and PLSQR_OK when the driver has none. */

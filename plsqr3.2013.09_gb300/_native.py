@@ -7,12 +7,14 @@ There is no fallback: a missing library raises at load time.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
 LIB_DIR = Path(__file__).resolve().parent / "lib"
-LIB_PATH = LIB_DIR / "libplsqr_gpu.so"
+# PLSQR_LIB: another build of the library (the bounds-checked one)
+LIB_PATH = Path(os.environ["PLSQR_LIB"]) if os.environ.get("PLSQR_LIB") else LIB_DIR / "libplsqr_gpu.so"
 
 PLSQR_OK = 0
 ERR = {
@@ -103,6 +105,7 @@ ITER_DTYPE = np.dtype([(k, "<f8") for k in ("alpha", "beta", "rnorm", "arnorm", 
 SIGNATURES = {
     "plsqr_strerror": (C.c_char_p, [C.c_int]),
     "plsqr_abi_version": (C.c_int, []),
+    "plsqr_check_flags": (C.c_int, [C.POINTER(i32), C.POINTER(C.c_uint32), i32]),
     "plsqr_default_opts": (None, [C.POINTER(Opts)]),
     "plsqr_default_lsqr_args": (None, [C.POINTER(LsqrArgs)]),
     "plsqr_device_count": (C.c_int, [C.POINTER(i32)]),
@@ -221,6 +224,14 @@ def device_count() -> int:
     n = i32(0)
     check(lib().plsqr_device_count(C.byref(n)), "plsqr_device_count")
     return int(n.value)
+
+
+def check_flags(reset: bool = False) -> tuple[bool, int]:
+    """(bounds-checked build?, the checks that failed on the current device)."""
+    checked, flags = i32(0), C.c_uint32(0)
+    check(lib().plsqr_check_flags(C.byref(checked), C.byref(flags), int(reset)),
+          "plsqr_check_flags")
+    return bool(checked.value), int(flags.value)
 
 
 def batch_variant(index: int) -> tuple[int, int, int]:

@@ -40,8 +40,8 @@ def _common() -> list[str]:
             "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off,-Wall,-Wno-unknown-pragmas"]
 
 
-def _compile(src: Path, obj: Path) -> None:
-    cmd = [nvcc(), *ARCH, "-lineinfo", *_common(), "-c", str(src), "-o", str(obj)]
+def _compile(src: Path, obj: Path, defines: tuple[str, ...] = ()) -> None:
+    cmd = [nvcc(), *ARCH, "-lineinfo", *_common(), *defines, "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cu":
         cmd += ["-Xptxas", "-v"] if os.environ.get("PLSQR_PTXAS_VERBOSE") else []
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -58,24 +58,31 @@ def _stale(out: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force: bool = False) -> Path:
-    """Compile libplsqr_gpu.so and plsqr3_gpu; returns the library path."""
+def build(force: bool = False, check: bool = False) -> Path:
+    """Compile libplsqr_gpu.so and plsqr3_gpu; returns the library path.
+    check: the bounds-checked library instead (-DPLSQR_CHECK, objects in
+    lib/check/, lib/libplsqr_gpu_check.so; no program), for tests."""
     LIB.mkdir(exist_ok=True)
+    odir = LIB / "check" if check else LIB
+    odir.mkdir(exist_ok=True)
+    defines = ("-DPLSQR_CHECK",) if check else ()
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "plsqr_gpu.h"]
     srcs = [CSRC / s for s in CU_SOURCES + CPP_SOURCES]
-    objs = [LIB / (s.name + ".o") for s in srcs]
+    objs = [odir / (s.name + ".o") for s in srcs]
     jobs = [(s, o) for s, o in zip(srcs, objs) if force or _stale(o, [s, *headers])]
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
-            for f in [ex.submit(_compile, s, o) for s, o in jobs]:
+            for f in [ex.submit(_compile, s, o, defines) for s, o in jobs]:
                 f.result()
-    so = LIB / LIBNAME
+    so = LIB / ("libplsqr_gpu_check.so" if check else LIBNAME)
     if force or jobs or _stale(so, objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(so), *map(str, objs),
                "-Xcompiler", "-fopenmp", "-lgomp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if check:
+        return so
     exe = LIB / "plsqr3_gpu"
     main_c = CSRC / "plsqr3_main.c"
     if force or _stale(exe, [main_c, so, INCLUDE / "plsqr_gpu.h"]):

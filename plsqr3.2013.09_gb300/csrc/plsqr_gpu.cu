@@ -276,7 +276,7 @@ template int slab_set_smem<float>(size_t);
 template <typename T>
 void units_spmv(const DevUnitsT<T> &U, const T *x, cudaStream_t s, const T *x_lo) {
   const UnitsArgs<T> A{U.idx,     U.val,     U.slot0,  U.q,     U.c,       U.line,       U.unit_begin,
-                       U.n_lines, U.n_slabs, U.slab,   U.n_idx, U.pf_dist, U.pf_pieces};
+                       U.n_lines, U.n_slabs, U.slab,   U.n_idx, U.pf_dist, U.pf_pieces, U.slots};
   cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
   if constexpr (sizeof(T) == 4) {
     if (x_lo && U.hilo) {
@@ -595,6 +595,20 @@ const char *plsqr_strerror(int code) {
 }
 
 int plsqr_abi_version(void) { return PLSQR_GPU_ABI_VERSION; }
+
+int plsqr_check_flags(int32_t *checked, uint32_t *flags, int32_t reset) {
+  if (!checked || !flags) return PLSQR_ERR_ARG;
+#ifdef PLSQR_CHECK
+  *checked = 1;
+#else
+  *checked = 0;
+#endif
+  // the unit kernels run in this translation unit, their fill and reorder in slab.cu
+  const unsigned a = plsqr::check_word(reset != 0), b = slab_check_word(reset != 0);
+  if (a == ~0u || b == ~0u) return PLSQR_ERR_CUDA;
+  *flags = a | b;
+  return PLSQR_OK;
+}
 
 void plsqr_default_opts(plsqr_opts *o) {
   if (!o) return;

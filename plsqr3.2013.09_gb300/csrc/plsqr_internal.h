@@ -142,6 +142,8 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
 // shared memory
 template <typename T>
 bool units_fit(int32_t n_idx, int32_t slab, bool hilo = false);
+// slab.cu: the bounds-check word of its kernels (check.cuh)
+unsigned slab_check_word(bool reset);
 // plsqr_gpu.cu: unit product launch and its shared-memory attribute
 // x_lo (FP32 layouts built with hilo): the low halves of the pairs x + x_lo
 template <typename T>

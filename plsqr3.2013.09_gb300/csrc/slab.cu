@@ -224,7 +224,7 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   CK(cudaMemcpy(d_seg_pos, seg_pos.data(), sizeof(int32_t) * seg_pos.size(), cudaMemcpyHostToDevice));
   const UnitsArgs<T> U{out->idx,       out->val, out->slot0, out->q, out->c, out->line,
                        out->unit_begin, n_lines,  n_slabs,    slab,   n_idx,  0,
-                       0};
+                       0,               slots};
   k_units_fill<<<g, 256, 0, ctx->stream>>>(L.ptr, L.idx, L.val, n_lines, n_slabs, slab, d_seg_unit,
                                            d_seg_pos, U, out->idx, out->val);
   CK(cudaGetLastError());
@@ -285,6 +285,8 @@ bool units_fit(int32_t n_idx, int32_t slab, bool hilo) {
   const size_t smem = hilo && sizeof(T) == 4 ? units_smem<T, true>(e, 1024) : units_smem<T, false>(e, 1024);
   return slab >= 1 && slab <= 65536 && (n_idx + slab - 1) / slab <= kMaxSlabs && smem <= 227 * 1024;
 }
+unsigned slab_check_word(bool reset) { return plsqr::check_word(reset); }
+
 template bool units_fit<double>(int32_t, int32_t, bool);
 template bool units_fit<float>(int32_t, int32_t, bool);
 

@@ -29,6 +29,7 @@
 
 #include <type_traits>
 
+#include "check.cuh"
 #include "slab.cuh"
 
 namespace plsqr {
@@ -47,7 +48,15 @@ struct UnitsArgs {
   int32_t n_lines, n_slabs, slab, n_idx;
   int32_t pf_dist;    // steps ahead of the L2 prefetch (0: none)
   int32_t pf_pieces;  // value pieces prefetched per lane: 1 or all P
+  int64_t n_slots;    // slots of the layout (bounds of the checked build)
 };
+
+// The 8 slab-local indices of a group, all inside the staged slab of len.
+__device__ __forceinline__ bool group_in(uint4 g, int len) {
+  const unsigned m = max(max(max(g.x & 0xffffu, g.x >> 16), max(g.y & 0xffffu, g.y >> 16)),
+                         max(max(g.z & 0xffffu, g.z >> 16), max(g.w & 0xffffu, g.w >> 16)));
+  return m < (unsigned)len;
+}
 
 // Values per 16-byte piece of a group, and pieces per group.
 template <typename T>
@@ -79,6 +88,7 @@ __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__r
       const int64_t j = t / q, k = t - j * q;
       const int64_t base = U.slot0[u];
       const int w = (int)(o & 7);
+      if (!chk(k < q && j < 32 && base + k * 32 + j < U.n_slots, kChkFill)) continue;
       sidx[(base + k * 32 + j) * 8 + w] = (uint16_t)(idx[e] - s * slab);
       sval[(base * P + (k * P + w / E) * 32 + j) * E + w % E] = (T)val[e];
     }
@@ -109,6 +119,7 @@ __global__ void k_units_banks(UnitsArgs<T> U, int n_units, int lanes_per_wave,
   for (int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n_units; u += warps) {
     const int q = U.q[u];
     const int64_t base = U.slot0[u];
+    if (!chk(base + (int64_t)q * 32 <= U.n_slots, kChkFill)) continue;
     for (int k = lane; k < q; k += 32)
       for (int h = 0; h < 32; h += lanes_per_wave) {
         uint16_t id[32][8];
@@ -312,9 +323,10 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
       const int G = c[kUnitLines];
       const int sj = lane * q;
       int li = kUnitLines, nb = 0x7fffffff;
+      chk(base + (int64_t)q * 32 <= A.n_slots, kChkSlot);
       if (sj < G) {  // the line holding this lane's first group (empty lines skipped)
         li = 0;
-        while (c[li + 1] <= sj) ++li;
+        while (c[li + 1] <= sj && chk(li + 1 < kUnitLines, kChkLine)) ++li;
         nb = c[li + 1];
       }
       const int li_first = li;
@@ -326,10 +338,10 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
         if (t == nb && t < G) {  // this lane's run enters the next line
           const double a = acc.total();
           if (li == li_first) p_first = a;
-          else part[ln[li]] = a;  // a line wholly inside the run
+          else if (chk(ln[li] >= 0 && ln[li] < A.n_lines, kChkLine)) part[ln[li]] = a;  // a line wholly inside the run
           acc.reset();
           ++li;
-          while (c[li + 1] <= t) ++li;
+          while (chk(li < kUnitLines, kChkLine) && c[li + 1] <= t) ++li;
           nb = c[li + 1];
         }
         const int kp = k + A.pf_dist;
@@ -339,10 +351,11 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(val16 + base * P +
                                                           (int64_t)(kp * P + pc) * 32 + lane));
         }
+        if (!chk(base + (int64_t)k * 32 + lane < A.n_slots, kChkSlot)) continue;
         const uint4 g = __ldg(idx8 + base + (int64_t)k * 32 + lane);
         T v[8];
         unit_vals(A.val, base, k, lane, v);
-        acc.add8(v, xs, g);
+        if (chk(group_in(g, len), kChkGather)) acc.add8(v, xs, g);
       }
       if (sj < G) {
         const double a = acc.total();
@@ -360,13 +373,14 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads)
       __syncwarp();
       // line `lane` of the unit: its parts in lane order
       const int l = ln[lane];
-      if (l >= 0) {
+      if (l >= 0 && chk(l < A.n_lines, kChkLine)) {
         const int c0 = c[lane], c1 = c[lane + 1];
         if (c0 == c1) {
           part[l] = 0;
         } else {
           const int a = c0 / q, b = (c1 - 1) / q;
-          if (a != b || lf[a] == lane || ll[a] == lane) {
+          if (!chk(a >= 0 && b < 32 && a <= b, kChkLane)) {
+          } else if (a != b || lf[a] == lane || ll[a] == lane) {
             double t = lf[a] == lane ? pf[a] : pl[a];
             for (int j = a + 1; j <= b; ++j) t += lf[j] == lane ? pf[j] : pl[j];
             part[l] = t;
