@@ -714,7 +714,21 @@ def bench_batched(pkg, args, device) -> dict:
                           "solver": "mixed precision, one right-hand side", "seconds": tm})
             grouped += tm
         cm.close()
-        out.update(value=grouped, timed_instances=len(timed),
+        # (c) retirement: the timed instances in one batch, each leaving as it
+        # comes within tol (checked every 16 iterations), the rest packed into
+        # the narrowest block that holds them; no counts known in advance
+        tb = b[timed]
+        rts = [ctx.batch_lsqr(tb, lam=[lam[j] for j in timed], x_ref=X[timed], sweeps=1,
+                              inner=inner, retire_every=16, retire_err=tol) for _ in range(2)]
+        rt = min(rts, key=lambda r: r["results"][0]["seconds"])
+        rt_err = [float(np.linalg.norm(rt["x"][i] - X[j]) / np.linalg.norm(X[j]))
+                  for i, j in enumerate(timed)]
+        retire = {"seconds": rt["results"][0]["seconds"], "check_every": 16,
+                  "iterations": {per[j]["name"]: rt["results"][i]["itn"]
+                                 for i, j in enumerate(timed)},
+                  "max_error": max(rt_err),
+                  "speedup_vs_fp64_sequential": fp64_total / rt["results"][0]["seconds"]}
+        out.update(value=grouped, timed_instances=len(timed), retire=retire,
                    fp64_sequential_seconds=fp64_total,
                    speedup_vs_fp64_sequential=fp64_total / grouped,
                    lock_step={"seconds": lock, "iterations": K,
@@ -724,7 +738,9 @@ def bench_batched(pkg, args, device) -> dict:
                         "tolerance, each group run as one batch (one sweep, to its slowest "
                         "member) or, a group of one, on the mixed-precision solver; device "
                         "time summed; lock_step: all 32 right-hand sides in one batch until "
-                        "the slowest timed one is within the tolerance; "
+                        "the slowest timed one is within the tolerance; retire: the timed "
+                        "ones in one batch, each retiring as it comes within the tolerance "
+                        "and the rest packed into narrower blocks; "
                         "fp64_sequential_seconds: the timed instances one after another on "
                         "the plain FP64 path")
     else:

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PLSQR_GPU_ABI_VERSION 3
+#define PLSQR_GPU_ABI_VERSION 4
 
 /* ---- error codes ------------------------------------------------------- */
 #define PLSQR_OK 0
@@ -308,7 +308,19 @@ typedef struct {
   int32_t variant_rows;  /* product variant of A x (plsqr_batch_variant), or
                             -1 = pick by timing (cached per operator shape)  */
   int32_t variant_cols;  /* the same for A^T y                                */
-  int32_t pad;
+  int32_t retire_every;  /* 0: every right-hand side runs sweeps*inner
+                            iterations.  R > 0: every R inner iterations the
+                            finished right-hand sides retire: with
+                            retire_err > 0 (needs x_ref) those with err <=
+                            retire_err, in any sweep; else those whose
+                            stopping test has fired (istop != 0) in the last
+                            sweep (conlim = 100, the reference's constant,
+                            fires once cond(A) passes 100: set conlim to
+                            suit).  A retiree's x and result are kept as they
+                            stand (result itn = the iteration it retired at;
+                            history records up to it), and the others go on
+                            packed into the narrowest block width that holds
+                            them.  The solve ends when none is left.        */
   double damp, atol, btol, conlim; /* lsqr() arguments of every solve; damp > 0
                                       requires sweeps = 1                    */
   const double *b_k;     /* [k][m_k]: right-hand side j at b_k + j*m_k        */
@@ -320,6 +332,7 @@ typedef struct {
                             right-hand side whose starting residual is not
                             below ||b|| starts from 0 instead (cold start);
                             info.warm says which kept x0.  Needs damp = 0.   */
+  double retire_err;     /* see retire_every; 0 = retire on istop         */
 } plsqr_batch_args;
 void plsqr_default_batch_args(plsqr_batch_args *a);
 

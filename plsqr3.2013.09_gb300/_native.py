@@ -76,9 +76,9 @@ class SynthParams(C.Structure):
 
 class BatchArgs(C.Structure):
     _fields_ = [("k", i32), ("sweeps", i32), ("inner", i32), ("variant_rows", i32),
-                ("variant_cols", i32), ("pad", i32), ("damp", f64), ("atol", f64),
+                ("variant_cols", i32), ("retire_every", i32), ("damp", f64), ("atol", f64),
                 ("btol", f64), ("conlim", f64), ("b_k", vp), ("lambda_", vp), ("x_ref", vp),
-                ("x0", vp)]
+                ("x0", vp), ("retire_err", f64)]
 
 
 class BatchInfo(C.Structure):

@@ -60,6 +60,7 @@ struct BatchState {
   double *U = nullptr, *V = nullptr, *W = nullptr, *X = nullptr, *DX = nullptr;
   double *B = nullptr, *XR = nullptr, *LAM = nullptr, *stage = nullptr;
   float *Uf = nullptr, *Vf = nullptr;
+  double *tmp = nullptr;  // repacking buffer of the retirement (max(m, n) * kp)
   DevState *st = nullptr;
   BatchCoef *cf = nullptr;
   double *parts = nullptr, *parts_dk = nullptr, *parts_err = nullptr;
@@ -241,9 +242,10 @@ void batch_free(plsqr_ctx *ctx) {
 
 static void free_vectors(plsqr_ctx *ctx, BatchState *B) {
   for (void *p : {(void *)B->U, (void *)B->V, (void *)B->W, (void *)B->X, (void *)B->DX,
-                  (void *)B->B, (void *)B->XR, (void *)B->stage, (void *)B->Uf, (void *)B->Vf})
+                  (void *)B->B, (void *)B->XR, (void *)B->stage, (void *)B->Uf, (void *)B->Vf,
+                  (void *)B->tmp})
     dev_free(ctx, p);
-  B->U = B->V = B->W = B->X = B->DX = B->B = B->XR = B->stage = nullptr;
+  B->U = B->V = B->W = B->X = B->DX = B->B = B->XR = B->stage = B->tmp = nullptr;
   B->Uf = B->Vf = nullptr;
   B->kp = 0;
 }
@@ -514,6 +516,8 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
                                 plsqr_iter *hist, plsqr_result *res, plsqr_batch_info *info) {
   if (!ctx || !a || !a->b_k) return PLSQR_ERR_ARG;
   if (a->k < 1 || a->k > kBatchMax || a->sweeps < 1 || a->inner < 1) return PLSQR_ERR_ARG;
+  if (a->retire_every < 0 || !(a->retire_err >= 0.0) || (a->retire_err > 0.0 && !a->x_ref))
+    return PLSQR_ERR_ARG;
   // as in the mixed solver: a damped sweep regularises the correction, not
   // the solution, so damp > 0 allows one sweep only
   if (a->damp != 0.0 && (a->sweeps > 1 || a->x0)) {
@@ -553,6 +557,11 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
   B->has_ref = a->x_ref != nullptr;
   const int64_t n = ctx->n, mk = ctx->m_k, m = mk + ctx->m_d;
   cudaStream_t s = ctx->stream;
+  const int R = a->retire_every;
+  if (R > 0 && !B->tmp) {
+    const size_t big = std::max(std::max((size_t)m, (size_t)n), (size_t)1);
+    if ((rc = dev_alloc(ctx, &B->tmp, big * B->kp))) return rc;
+  }
   // inputs: right-hand sides, weights, reference solutions
   std::vector<double> lam(kBatchMax, 1.0);
   for (int j = 0; j < k; ++j) lam[(size_t)j] = a->lambda ? a->lambda[j] : 1.0;
@@ -603,18 +612,45 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
     B->hist_cap = (int64_t)k * (total + 1);
   }
   CK(cudaMemsetAsync(B->hist, 0, sizeof(plsqr_iter) * k * (total + 1), s));
+  // product variants: of the narrower widths a retirement may pack into
+  // (cached per operator shape, else timed here, before the timed solve),
+  // then of the starting width
+  std::map<int, std::pair<int, int>> width_var;
+  if (R > 0)
+    for (int kq = 4; kq < kw; kq *= 2) {
+      B->kw = kq;
+      B->k = std::min(k, kq);
+      // the caller's variants where they suit the narrower block
+      const int vr = variant_ok(a->variant_rows, kq) ? a->variant_rows : -1;
+      const int vc = variant_ok(a->variant_cols, kq) ? a->variant_cols : -1;
+      if ((rc = batch_choose(ctx, vr, vc))) return rc;
+      width_var[kq] = std::make_pair(B->var_rows, B->var_cols);
+    }
+  B->kw = kw;
+  B->k = k;
   if ((rc = batch_choose(ctx, a->variant_rows, a->variant_cols))) return rc;
+  const int tuned = B->tuned;
+  const double ms_rows = B->ms_rows, ms_cols = B->ms_cols;
+  width_var[kw] = std::make_pair(B->var_rows, B->var_cols);
   if ((rc = ensure_graph(ctx, B))) return rc;
+  // ka right-hand sides active in a block of width kwa; block column j holds
+  // the caller's right-hand side orig[j]
+  int ka = k, kwa = kw;
+  ColMap orig;
+  for (int j = 0; j < kBatchMax; ++j) orig.c[j] = j < k ? j : 0;
+  std::vector<DevState> fin((size_t)k);
+  std::vector<int> fin_itn((size_t)k, -1);
   std::vector<plsqr_iter> h0((size_t)k);
   std::vector<DevState> cur((size_t)k);
   memset(h0.data(), 0, sizeof(plsqr_iter) * k);
   int last_itn = 0;
+  bool finished = false;
   CK(cudaEventRecord(ctx->ev0, s));
-  for (int sw = 0; sw < S; ++sw) {
+  for (int sw = 0; sw < S && !finished; ++sw) {
    for (int attempt = 0; attempt < 2; ++attempt) {
-    std::vector<DevState> h((size_t)k);
-    memset(h.data(), 0, sizeof(DevState) * k);
-    for (int j = 0; j < k; ++j) {
+    std::vector<DevState> h((size_t)ka);
+    memset(h.data(), 0, sizeof(DevState) * ka);
+    for (int j = 0; j < ka; ++j) {
       DevState &d = h[(size_t)j];
       d.damp = a->damp;
       d.atol = a->atol;
@@ -624,21 +660,23 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
       d.has_ref = B->has_ref;
       d.cs2 = -1.0;
       d.hist_base = sw * I;
+      d.slot = orig.c[j];
+      d.err = -1.0;
     }
-    CK(cudaMemcpyAsync(B->st, h.data(), sizeof(DevState) * k, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(B->st, h.data(), sizeof(DevState) * ka, cudaMemcpyHostToDevice, s));
     if (B->has_ref)
-      k_bref_norm<<<B->gvec, kBatchThreads, 0, s>>>(B->XR, ctx->n, kw, k, B->st, B->cf, B->parts);
+      k_bref_norm<<<B->gvec, kBatchThreads, 0, s>>>(B->XR, ctx->n, kwa, ka, B->st, B->cf, B->parts);
     // outer residual and the start-up of the correction solves
-    k_bresidual<<<B->gres, kBatchThreads, 0, s>>>(ctx->K.csr(), ctx->D.csr(), kw, k, B->X, B->B,
+    k_bresidual<<<B->gres, kBatchThreads, 0, s>>>(ctx->K.csr(), ctx->D.csr(), kwa, ka, B->X, B->B,
                                                    B->U, B->LAM, B->st, B->cf, B->parts);
-    k_bscale_u<<<B->gvec, kBatchThreads, 0, s>>>(B->U, B->Uf, mk, m, kw, B->cf);
-    CK(cudaMemsetAsync(B->V, 0, sizeof(double) * n * kw, s));
+    k_bscale_u<<<B->gvec, kBatchThreads, 0, s>>>(B->U, B->Uf, mk, m, kwa, B->cf);
+    CK(cudaMemsetAsync(B->V, 0, sizeof(double) * n * kwa, s));
     kVariants[B->var_cols].cols(ctx, *B, kScaleZero, s);
     k_bupdate<<<B->gvec, kBatchThreads, 0, s>>>(B->V, B->Vf, B->W, B->DX, B->X, nullptr, ctx->n,
-                                                 kw, k, B->cf, B->st, B->parts_dk, B->parts_err,
+                                                 kwa, ka, B->cf, B->st, B->parts_dk, B->parts_err,
                                                  1, nullptr, 1);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * k, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * ka, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (sw == 0 && attempt == 0 && a->x0) {
       // cold start where x0 does not lower the residual: ||[b; 0] - A x0|| >= ||b||
@@ -657,50 +695,130 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
     break;
    }
     bool all_done = true;
-    for (int j = 0; j < k; ++j) {
+    for (int j = 0; j < ka; ++j) {
       const DevState &c = cur[(size_t)j];
       all_done = all_done && c.done;
       if (sw == 0) {
-        plsqr_iter &e = h0[(size_t)j];
+        plsqr_iter &e = h0[(size_t)orig.c[j]];
         e.alpha = c.alpha;
         e.beta = c.beta;
         e.rnorm = c.beta;
         e.arnorm = c.arnorm;
         e.test1 = 1.0;
         e.test2 = c.beta > 0.0 ? c.alpha / c.beta : 0.0;
-        e.err = B->has_ref ? err0[(size_t)j] : -1.0;
+        e.err = B->has_ref ? err0[(size_t)orig.c[j]] : -1.0;
       }
     }
     if (all_done) break;  // A^T r_j = 0 for every j: X solves every problem
-    for (int i = 0; i < I; ++i) CK(cudaGraphLaunch(B->graph, s));
-    k_badd<<<gl, 256, 0, s>>>(B->X, B->DX, n * kw);
+    for (int i = 0; i < I;) {
+      const int step = R > 0 ? std::min(R, I - i) : I;
+      for (int t = 0; t < step; ++t) CK(cudaGraphLaunch(B->graph, s));
+      i += step;
+      last_itn = sw * I + i;
+      if (R <= 0 || i == I) continue;
+      // retirement: finished right-hand sides keep x = X + DX and their state
+      CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * ka, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      ColMap from;
+      int kn = 0;
+      for (int j = 0; j < ka; ++j) {
+        const DevState &c = cur[(size_t)j];
+        const bool stop = c.done || (a->retire_err > 0.0 ? c.err >= 0.0 && c.err <= a->retire_err
+                                                         : sw == S - 1 && c.istop != 0);
+        if (!stop) {
+          from.c[kn++] = j;
+          continue;
+        }
+        const int o = orig.c[j];
+        fin[(size_t)o] = c;
+        fin_itn[(size_t)o] = last_itn;
+        k_bput<<<gl, 256, 0, s>>>(B->X, B->DX, n, kwa, j, B->stage + (int64_t)o * n);
+      }
+      CK(cudaGetLastError());
+      if (kn == ka) continue;
+      if (kn == 0) {
+        finished = true;
+        ka = 0;
+        break;
+      }
+      // pack the kn that go on into the narrowest width that holds them
+      const int kq = width_for(kn);
+      struct Blk {
+        void *p;
+        int64_t rows;
+        bool f32;
+      };
+      const Blk blocks[] = {{B->U, m, false},   {B->V, n, false},  {B->W, n, false},
+                            {B->X, n, false},   {B->DX, n, false}, {B->B, mk, false},
+                            {B->XR, B->has_ref ? n : 0, false},    {B->Uf, mk, true},
+                            {B->Vf, n, true}};
+      for (const Blk &b : blocks) {
+        if (b.rows <= 0) continue;
+        const size_t bytes = (size_t)b.rows * kq * (b.f32 ? sizeof(float) : sizeof(double));
+        if (b.f32)
+          k_bcompact<float><<<gl, 256, 0, s>>>((const float *)b.p, (float *)B->tmp, b.rows, kwa,
+                                               kq, kn, from);
+        else
+          k_bcompact<double><<<gl, 256, 0, s>>>((const double *)b.p, B->tmp, b.rows, kwa, kq, kn,
+                                                from);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(b.p, B->tmp, bytes, cudaMemcpyDeviceToDevice, s));
+      }
+      std::vector<DevState> packed((size_t)kn);
+      std::vector<double> lam2(kBatchMax, 1.0);
+      ColMap orig2 = orig;
+      for (int j = 0; j < kn; ++j) {
+        packed[(size_t)j] = cur[(size_t)from.c[j]];
+        lam2[(size_t)j] = lam[(size_t)from.c[j]];
+        orig2.c[j] = orig.c[from.c[j]];
+      }
+      orig = orig2;
+      lam = lam2;
+      CK(cudaMemcpyAsync(B->st, packed.data(), sizeof(DevState) * kn, cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(B->LAM, lam.data(), sizeof(double) * kBatchMax, cudaMemcpyHostToDevice,
+                         s));
+      CK(cudaStreamSynchronize(s));  // the host vectors above are reused
+      ka = kn;
+      kwa = kq;
+      B->k = ka;
+      B->kw = kwa;
+      B->var_rows = width_var.at(kwa).first;
+      B->var_cols = width_var.at(kwa).second;
+      if ((rc = ensure_graph(ctx, B))) return rc;
+    }
+    if (finished) break;
+    k_badd<<<gl, 256, 0, s>>>(B->X, B->DX, n * kwa);
     CK(cudaGetLastError());
-    last_itn = (sw + 1) * I;
   }
   CK(cudaEventRecord(ctx->ev1, s));
   CK(cudaEventSynchronize(ctx->ev1));
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * k, cudaMemcpyDeviceToHost, s));
+  if (ka > 0)
+    CK(cudaMemcpyAsync(cur.data(), B->st, sizeof(DevState) * ka, cudaMemcpyDeviceToHost, s));
   if (hist) {
     CK(cudaMemcpyAsync(hist, B->hist, sizeof(plsqr_iter) * k * (total + 1), cudaMemcpyDeviceToHost,
                        s));
   }
-  if (x) {
-    k_bscatter<<<gl, 256, 0, s>>>(B->X, n, kw, k, B->stage, n);
+  if (ka > 0) {
+    k_bscatter<<<gl, 256, 0, s>>>(B->X, n, kwa, ka, orig, B->stage, n);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(x, B->stage, sizeof(double) * n * k, cudaMemcpyDeviceToHost, s));
   }
+  if (x) CK(cudaMemcpyAsync(x, B->stage, sizeof(double) * n * k, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  for (int j = 0; j < ka; ++j) {
+    fin[(size_t)orig.c[j]] = cur[(size_t)j];
+    fin_itn[(size_t)orig.c[j]] = last_itn;
+  }
   if (hist)
     for (int j = 0; j < k; ++j) hist[(int64_t)j * (total + 1)] = h0[(size_t)j];
   if (res) {
     for (int j = 0; j < k; ++j) {
-      const DevState &c = cur[(size_t)j];
+      const DevState &c = fin[(size_t)j];
       plsqr_result &r = res[j];
       memset(&r, 0, sizeof(r));
       r.istop = c.istop;
-      r.itn = last_itn;
+      r.itn = fin_itn[(size_t)j];
       r.anorm = c.anorm;
       r.acond = c.acond;
       r.rnorm = c.rnorm;
@@ -715,6 +833,13 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
       r.seconds_total = r.seconds;
     }
   }
+  B->tuned = tuned;
+  B->ms_rows = ms_rows;
+  B->ms_cols = ms_cols;
+  B->var_rows = width_var.at(kw).first;
+  B->var_cols = width_var.at(kw).second;
+  B->k = k;
+  B->kw = kw;
   fill_info(B, info);
   if (info) info->warm = (int32_t)warm;
   return PLSQR_OK;

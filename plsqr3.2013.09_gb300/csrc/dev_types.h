@@ -23,7 +23,8 @@ struct DevState {
   double s_alpha, s_rhobar, s_phibar, s_phi, s_rho, s_theta, s_tau, s_psi;
   int32_t s_beta_pos, done;
   int32_t hist_base;  // history index of this solve's iteration 0
-  int32_t pad0;
+  int32_t slot;       // batched solver: the right-hand side's history row
+  double err;         // ||x - x_ref|| / ||x_ref|| after the last iteration (-1: no x_ref)
 };
 
 // One compressed-sparse operand as the kernels see it, with values of type T

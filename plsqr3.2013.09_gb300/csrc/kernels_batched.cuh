@@ -440,6 +440,7 @@ static __global__ void __launch_bounds__(kBatchThreads)
 // start of its solve): the state as it is, one more iteration counted.
 __device__ __forceinline__ void batch_hist_idle(DevState &S, double err2, plsqr_iter *hist) {
   const int itn = S.itn + 1;
+  S.err = S.has_ref ? __dsqrt_rn(ddiv(err2, S.ref_norm2)) : -1.0;
   if (hist) {
     plsqr_iter &h = hist[S.hist_base + itn];
     h.alpha = S.alpha;
@@ -452,7 +453,7 @@ __device__ __forceinline__ void batch_hist_idle(DevState &S, double err2, plsqr_
     h.acond = S.acond;
     h.xnorm = S.xnorm;
     h.x0 = 0.0;
-    h.err = S.has_ref ? __dsqrt_rn(ddiv(err2, S.ref_norm2)) : -1.0;
+    h.err = S.err;
     h.istop = S.istop;
     h.pad = 0;
   }
@@ -464,7 +465,7 @@ __device__ __forceinline__ void batch_hist_idle(DevState &S, double err2, plsqr_
 // (source/lsqr.c:685-690); with a reference block, the squared error of
 // x_base + dx.  start = 1: w = v (where alpha_j > 0), dx = 0.  The last block
 // finishes each right-hand side's iteration (source/lsqr.c:703-775) and
-// writes its history record at hist[j*hist_stride + hist_base + itn].
+// writes its history record at hist[slot_j*hist_stride + hist_base + itn].
 static __global__ void __launch_bounds__(kBatchThreads)
     k_bupdate(double *__restrict__ v, float *__restrict__ vf, double *__restrict__ w,
               double *__restrict__ dx, const double *__restrict__ x_base,
@@ -515,7 +516,7 @@ static __global__ void __launch_bounds__(kBatchThreads)
     DevState &S = st[jj];
     const double d2 = batch_col_sum(parts_dk, gridDim.x, kp, jj);
     const double er = xref ? batch_col_sum(parts_err, gridDim.x, kp, jj) : 0.0;
-    plsqr_iter *h = hist ? hist + (int64_t)jj * hist_stride : nullptr;
+    plsqr_iter *h = hist ? hist + (int64_t)S.slot * hist_stride : nullptr;
     if (S.done)
       batch_hist_idle(S, er, h);
     else
@@ -604,14 +605,43 @@ static __global__ void k_bgather(const double *__restrict__ src, int64_t ld, int
     dst[i] = j < k ? src[(int64_t)j * ld + r] : 0.0;
   }
 }
+// Block column j < k goes to host column to.c[j] (the right-hand side's
+// index in the caller's arrays).
+struct ColMap {
+  int32_t c[kBatchMax];
+};
 static __global__ void k_bscatter(const double *__restrict__ src, int64_t rows, int kp, int k,
-                           double *__restrict__ dst, int64_t ld) {
+                                  ColMap to, double *__restrict__ dst, int64_t ld) {
   const int64_t total = rows * kp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = i / kp;
     const int j = (int)(i - r * kp);
-    if (j < k) dst[(int64_t)j * ld + r] = src[i];
+    if (j < k) dst[(int64_t)to.c[j] * ld + r] = src[i];
+  }
+}
+
+// dst[r] = x[r*kp + j] + dx[r*kp + j]: the solution of a right-hand side
+// retired in the middle of a sweep (the sweep's correction added as X += DX
+// adds it at the sweep's end).
+static __global__ void k_bput(const double *__restrict__ x, const double *__restrict__ dx,
+                              int64_t rows, int kp, int j, double *__restrict__ dst) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows;
+       r += (int64_t)gridDim.x * blockDim.x)
+    dst[r] = x[r * kp + j] + dx[r * kp + j];
+}
+
+// Repacking of a block after retirements: dst[r*kq + j] = src[r*kp + from.c[j]]
+// for the k right-hand sides kept (j < k), 0 in the padding columns.
+template <typename V>
+static __global__ void k_bcompact(const V *__restrict__ src, V *__restrict__ dst, int64_t rows,
+                                  int kp, int kq, int k, ColMap from) {
+  const int64_t total = rows * kq;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / kq;
+    const int j = (int)(i - r * kq);
+    dst[i] = j < k ? src[r * kp + from.c[j]] : V(0);
   }
 }
 

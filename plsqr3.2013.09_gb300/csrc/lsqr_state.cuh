@@ -106,6 +106,7 @@ __device__ __forceinline__ void lsqr_tail(DevState &s, double dknorm2, double er
   if (s.test2 <= s.atol) istop = 2;
   if (s.test1 <= rtol) istop = 1;
   s.istop = istop;
+  s.err = s.has_ref ? __dsqrt_rn(ddiv(err2, s.ref_norm2)) : -1.0;
   if (hist) {
     plsqr_iter &h = hist[s.hist_base + itn];
     h.alpha = s.alpha;
@@ -118,7 +119,7 @@ __device__ __forceinline__ void lsqr_tail(DevState &s, double dknorm2, double er
     h.acond = s.acond;
     h.xnorm = s.xnorm;
     h.x0 = x0;
-    h.err = s.has_ref ? __dsqrt_rn(ddiv(err2, s.ref_norm2)) : -1.0;
+    h.err = s.err;
     h.istop = istop;
     h.pad = 0;
   }

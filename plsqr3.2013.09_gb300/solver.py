@@ -188,15 +188,20 @@ class Context:
     def batch_lsqr(self, b_k, *, lam=None, x_ref=None, x0=None, sweeps: int = 4, inner: int = 50,
                    damp: float = 0.0, atol: float = 1e-10, btol: float = 1e-10,
                    conlim: float = 100.0, variant_rows: int = -1,
-                   variant_cols: int = -1) -> dict:
+                   variant_cols: int = -1, retire_every: int = 0,
+                   retire_err: float = 0.0) -> dict:
         """k <= 32 solves in lock step, one k-wide product per matrix read.
 
         b_k: (k, m_k) right-hand sides; lam: (k,) damping-row weights (solve j
         uses [K; lam_j D]); x_ref: (k, n) solutions for the history's err
         field; x0: (k, n) starting solutions (warm start, with the cold start
         as fallback where b - A x0 is not smaller than b; info["warm"] has bit
-        j set where x0 was kept).  Returns x (k, n), hist (k, sweeps*inner + 1), per-solve
-        results and the product variants used."""
+        j set where x0 was kept).  retire_every = R > 0: every R iterations
+        the finished solves (err <= retire_err with x_ref where retire_err >
+        0, else LSQR's own stop in the last sweep) retire with their x and
+        result as they stand (result "itn": the iteration they retired at)
+        and the rest go on in a block no wider than they need.  Returns x (k, n), hist (k,
+        sweeps*inner + 1), per-solve results and the product variants used."""
         b = np.ascontiguousarray(b_k, np.float64)
         if b.ndim != 2 or b.shape[1] != self.m_k:
             raise ValueError(f"b_k must have shape (k, {self.m_k}), got {b.shape}")
@@ -214,6 +219,7 @@ class Context:
         N.lib().plsqr_default_batch_args(C.byref(a))
         a.k, a.sweeps, a.inner = k, sweeps, inner
         a.variant_rows, a.variant_cols = variant_rows, variant_cols
+        a.retire_every, a.retire_err = retire_every, retire_err
         a.damp, a.atol, a.btol, a.conlim = damp, atol, btol, conlim
         a.b_k, a.lambda_, a.x_ref, a.x0 = N.ptr(b), N.ptr(lm), N.ptr(xr), N.ptr(xs)
         x = np.empty((k, self.n))

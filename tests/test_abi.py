@@ -54,7 +54,7 @@ def test_struct_sizes_match_header(pkg):
 
 def test_strerror_and_version(pkg):
     L = pkg._native.lib()
-    assert L.plsqr_abi_version() == 3
+    assert L.plsqr_abi_version() == 4
     assert L.plsqr_strerror(0) == b"success"
     assert L.plsqr_strerror(-3) == b"file or matrix content is inconsistent"
     assert L.plsqr_strerror(-99) == b"unknown error"

@@ -189,3 +189,127 @@ def test_warm_start_and_cold_fallback(pkg, grid32):
     # the far start fell back: the same bits as the cold solve
     assert np.array_equal(back["x"][1], cold["x"][1])
     assert np.array_equal(back["x"][0], warm["x"][0])
+
+
+def first_at_or_below(err, tol, start=1):
+    idx = np.nonzero(err[start:] <= tol)[0]
+    return None if idx.size == 0 else int(idx[0]) + start
+
+
+def test_retirement_on_error_packs_the_rest(pkg, grid32):
+    """retire_every / retire_err: every R iterations the right-hand sides
+    within retire_err of x_ref leave with x = X + DX and their state, the
+    others go on in a narrower block.  Up to the first retirement the run is
+    the lock-step run bit for bit; every retiree is within the tolerance at
+    its retirement and was not at the check before; the ones that never get
+    there end where the lock-step run ends, to the rounding of the narrower
+    blocks' products."""
+    prob, insts = grid32
+    # the 32 instances come within 1e-5 between iterations 73 and 80: a check
+    # every iteration retires them over several checks, packing 32 -> 16 -> 8
+    # -> 4
+    tol, R, inner = 1e-5, 1, 600
+    b = np.stack([i.b_k for i in insts])
+    lam = [i.lam for i in insts]
+    xstar = np.stack([fp64_solution(pkg, prob, i, 800)["x"] for i in insts])
+    kw = dict(lam=lam, x_ref=xstar, sweeps=1, inner=inner, variant_rows=1, variant_cols=1)
+    with pkg.Context(prob) as ctx:
+        lock = ctx.batch_lsqr(b, **kw)
+        ret = ctx.batch_lsqr(b, retire_every=R, retire_err=tol, **kw)
+    err_l, err_r = lock["hist"]["err"], ret["hist"]["err"]
+    ks = [first_at_or_below(err_l[j], tol) for j in range(len(insts))]
+    reached = [j for j, k in enumerate(ks) if k is not None and k < inner - 2 * R]
+    assert len(reached) >= 16
+    t1 = min(-(-ks[j] // R) * R for j in reached)
+    assert np.array_equal(ret["hist"][:, :t1 + 1], lock["hist"][:, :t1 + 1])
+    itns = [r["itn"] for r in ret["results"]]
+    left_at = set()
+    for j in range(len(insts)):
+        it = itns[j]
+        if err_l[j][t1] <= tol:
+            assert it == t1, (insts[j].name, it, t1)
+        if it < inner:
+            left_at.add(it)
+            assert it % R == 0
+            assert err_r[j][it] <= tol
+            if it > R:
+                assert err_r[j][it - R] > tol
+            assert rel(ret["x"][j], xstar[j]) <= tol * (1 + 1e-9)
+            assert np.all(ret["hist"][j][it + 1:]["beta"] == 0.0)
+        else:
+            e_l, e_r = err_l[j][inner], err_r[j][inner]
+            assert abs(e_r - e_l) <= 0.1 * e_l, (insts[j].name, e_l, e_r)
+            assert rel(ret["x"][j], xstar[j]) == pytest.approx(e_r, rel=1e-6)
+    # retirements at several checks: the block was packed more than once
+    assert len(left_at) >= 3
+    assert ret["results"][0]["seconds"] > 0
+    assert ret["info"]["k"] == len(insts) and ret["info"]["kp"] == 32
+
+
+def test_retirement_on_lsqr_stop(pkg, grid32):
+    """Without x_ref a right-hand side retires on LSQR's own stopping test
+    (istop != 0) in the last sweep; the retirees' results carry that istop
+    and the iteration they left at.  (conlim = 0: no condition-number stop,
+    which at the default conlim = 100 would end these solves at once.)"""
+    prob, insts = grid32
+    sel = pkg.batch.pick(insts, 8)
+    b = np.stack([i.b_k for i in sel])
+    R, inner = 8, 800
+    kw = dict(lam=[i.lam for i in sel], sweeps=1, inner=inner, atol=1e-5, btol=1e-5,
+              conlim=0.0, variant_rows=1, variant_cols=1)
+    with pkg.Context(prob) as ctx:
+        lock = ctx.batch_lsqr(b, **kw)
+        ret = ctx.batch_lsqr(b, retire_every=R, **kw)
+    stop = []
+    for j in range(len(sel)):
+        nz = np.nonzero(lock["hist"]["istop"][j][1:])[0]
+        stop.append(int(nz[0]) + 1 if nz.size else None)
+    stopped = [j for j, s0 in enumerate(stop) if s0 is not None and s0 < inner - 2 * R]
+    assert len(stopped) >= 4, stop
+    t1 = min(-(-stop[j] // R) * R for j in stopped)
+    assert np.array_equal(ret["hist"][:, :t1 + 1], lock["hist"][:, :t1 + 1])
+    for j in range(len(sel)):
+        r = ret["results"][j]
+        if r["itn"] == inner:
+            assert j not in stopped or -(-stop[j] // R) * R != t1
+            continue
+        assert r["istop"] != 0 and r["itn"] % R == 0, (sel[j].name, r)
+        assert ret["hist"]["istop"][j][r["itn"]] != 0
+        if r["itn"] > R:
+            assert ret["hist"]["istop"][j][r["itn"] - R] == 0
+        if stop[j] is not None and -(-stop[j] // R) * R == t1:
+            assert r["itn"] == t1
+    if all(r["itn"] < inner for r in ret["results"]):
+        # everything retired before the limit: less device time
+        assert ret["results"][0]["seconds"] < lock["results"][0]["seconds"]
+
+
+def test_retirement_across_sweeps(pkg, grid32):
+    """Error retirement in any refinement sweep: a retiree's x is X + DX of
+    its sweep, the rest go on through the following sweeps."""
+    prob, insts = grid32
+    sel = pkg.batch.pick(insts, 12)
+    tol = 3e-6
+    xstar = np.stack([fp64_solution(pkg, prob, i, 800)["x"] for i in sel])
+    kw = dict(lam=[i.lam for i in sel], x_ref=xstar, sweeps=4, inner=60, variant_rows=1,
+              variant_cols=1)
+    b = np.stack([i.b_k for i in sel])
+    with pkg.Context(prob) as ctx:
+        lock = ctx.batch_lsqr(b, **kw)
+        ret = ctx.batch_lsqr(b, retire_every=15, retire_err=tol, **kw)
+        with pytest.raises(pkg._native.PlsqrError):
+            ctx.batch_lsqr(b, retire_every=-1, **kw)
+        with pytest.raises(pkg._native.PlsqrError):
+            ctx.batch_lsqr(b, retire_every=5, retire_err=-1.0, **kw)
+        with pytest.raises(pkg._native.PlsqrError):
+            ctx.batch_lsqr(b, retire_every=5, retire_err=1e-6, sweeps=1, inner=10)
+    for j in range(len(sel)):
+        it = ret["results"][j]["itn"]
+        e = rel(ret["x"][j], xstar[j])
+        if it < 240:
+            assert e <= tol * (1 + 1e-9), (sel[j].name, it, e)
+            assert ret["hist"]["err"][j][it] <= tol
+        else:
+            e_l = rel(lock["x"][j], xstar[j])
+            assert abs(e - e_l) <= 0.1 * e_l + 1e-9, (sel[j].name, e, e_l)
+    assert min(r["itn"] for r in ret["results"]) < 240
