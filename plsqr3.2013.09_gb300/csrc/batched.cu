@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "kernels_batched.cuh"
+#include "kernels_bunits.cuh"
 #include "kernels_f32.cuh"
 #include "plsqr_internal.h"
 
@@ -83,6 +84,12 @@ struct BatchState {
     int g_rows = 0, g_cols = 0;
   };
   std::map<int, SlabPlan> slab;
+  // units form (blocks of 4 or 8): FP32 unit layouts of K by row and by
+  // column, one lane per line, and their k-wide partial sums
+  DevUnitsT<float> ur, uc;
+  bool units_tried = false, units_ok = false;
+  double *upart = nullptr;
+  int gur = 1, guc = 1;  // grids of the combine kernels
   int n_parts = 0;          // capacity of parts (per right-hand side)
   bool lines_sorted = true;  // every kernel row and column ascending (slab form)
 };
@@ -135,6 +142,43 @@ void launch_slab_cols(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_
   }
 }
 
+UnitsArgs<float> units_args(const DevUnitsT<float> &U) {
+  return UnitsArgs<float>{U.idx,     U.val,     U.slot0, U.q,     U.c,       U.line,       U.unit_begin,
+                          U.n_lines, U.n_slabs, U.slab,  U.n_idx, U.pf_dist, U.pf_pieces, U.slots};
+}
+template <int KW>
+size_t bunits_smem(const DevUnitsT<float> &U) {
+  return sizeof(float) * KW * (size_t)std::min(U.slab, U.n_idx);
+}
+template <int KW>
+void launch_units_rows_t(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  const DevUnitsT<float> &U = B.ur;
+  cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
+  k_bunits<KW><<<U.blocks, kBUnitThreads, bunits_smem<KW>(U), s>>>(units_args(U), U.next, B.Vf,
+                                                                   B.upart);
+  k_bunits_rows<KW><<<B.gur, kBatchThreads, 0, s>>>(B.upart, U.n_slabs, ctx->m_k, ctx->D.csr(),
+                                                     B.k, B.V, B.U, B.LAM, mode, B.st, B.cf,
+                                                     B.parts);
+}
+template <int KW>
+void launch_units_cols_t(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  const DevUnitsT<float> &U = B.uc;
+  cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
+  k_bunits<KW><<<U.blocks, kBUnitThreads, bunits_smem<KW>(U), s>>>(units_args(U), U.next, B.Uf,
+                                                                   B.upart);
+  k_bunits_cols<KW><<<B.guc, kBatchThreads, 0, s>>>(B.upart, U.n_slabs, ctx->DC.csr(), ctx->m_k,
+                                                     ctx->n, B.k, B.U, B.V, B.LAM, mode, B.st,
+                                                     B.cf, B.parts);
+}
+void launch_units_rows(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  if (B.kw == 4) return launch_units_rows_t<4>(ctx, B, mode, s);
+  return launch_units_rows_t<8>(ctx, B, mode, s);
+}
+void launch_units_cols(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
+  if (B.kw == 4) return launch_units_cols_t<4>(ctx, B, mode, s);
+  return launch_units_cols_t<8>(ctx, B, mode, s);
+}
+
 #define VARIANT(vw, lpr, u) \
   Variant { vw, lpr, u, launch_rows<vw, lpr, u>, launch_cols<vw, lpr, u> }
 // lpr = 0: the slab form (float4 gathers from shared memory, kw/4 lanes per
@@ -144,6 +188,8 @@ const Variant kVariants[] = {
     VARIANT(4, 32, 2), VARIANT(4, 32, 4), VARIANT(2, 16, 2), VARIANT(2, 16, 4),
     VARIANT(2, 32, 2), VARIANT(2, 32, 4), VARIANT(2, 8, 2),  VARIANT(2, 8, 4),
     Variant{4, 0, 0, launch_slab_rows, launch_slab_cols},
+    // lpr = -1: the units form (kernels_bunits.cuh), blocks of 4 or 8
+    Variant{4, -1, 0, launch_units_rows, launch_units_cols},
 };
 #undef VARIANT
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
@@ -152,6 +198,7 @@ bool variant_ok(int v, int kp) {
   if (v < 0 || v >= kNumVariants) return false;
   const Variant &V = kVariants[v];
   if (V.lpr == 0) return true;
+  if (V.lpr < 0) return kp == 4 || kp == 8;
   return kp % V.vw == 0 && kp / V.vw <= V.lpr;
 }
 
@@ -373,6 +420,58 @@ static int batch_setup(plsqr_ctx *ctx) {
   return PLSQR_OK;
 }
 
+// The units form's layouts, built on first use: slabs of kBUnitSlab rows of
+// the block (192 KB of shared memory at 8 right-hand sides), where both
+// dimensions fit the unit layout's slab count; PLSQR_BATCH_UNITS=0 leaves
+// them out.
+static int batch_units(plsqr_ctx *ctx) {
+  BatchState *B = ctx->batch;
+  if (B->units_tried) return PLSQR_OK;
+  B->units_tried = true;
+  const int S = kBUnitSlab;
+  if (const char *e = getenv("PLSQR_BATCH_UNITS"))
+    if (atoi(e) == 0) return PLSQR_OK;
+  if (ctx->nnz_k == 0 || !units_fit<float>(ctx->n, S) || !units_fit<float>(ctx->m_k, S))
+    return PLSQR_OK;
+  int rc;
+  if ((rc = build_units<float>(ctx, ctx->K, ctx->n, S, &B->ur, false, true)) ||
+      (rc = build_units<float>(ctx, ctx->KC, ctx->m_k, S, &B->uc, false, true)))
+    return rc;
+  // the k-wide partials replace the layouts' own
+  dev_free(ctx, B->ur.partial);
+  dev_free(ctx, B->uc.partial);
+  B->ur.partial = B->uc.partial = nullptr;
+  B->ur.blocks = B->uc.blocks = ctx->sm_count;
+  const size_t cells = std::max((size_t)B->ur.n_slabs * ctx->m_k, (size_t)B->uc.n_slabs * ctx->n);
+  if ((rc = dev_alloc(ctx, &B->upart, cells * 8))) return rc;
+  const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  CK(cudaFuncSetAttribute(k_bunits<4>, attr,
+                          (int)std::max(bunits_smem<4>(B->ur), bunits_smem<4>(B->uc))));
+  CK(cudaFuncSetAttribute(k_bunits<8>, attr,
+                          (int)std::max(bunits_smem<8>(B->ur), bunits_smem<8>(B->uc))));
+  B->gur = 8 * ctx->sm_count;
+  B->guc = 8 * ctx->sm_count;
+  B->units_ok = true;
+  return PLSQR_OK;
+}
+
+// Variant v can run on this operator at block width kp: the slab form needs
+// every line in ascending order, the units form its layouts (built here).
+static int variant_usable(plsqr_ctx *ctx, int v, int kp, bool *ok) {
+  *ok = variant_ok(v, kp);
+  if (!*ok) return PLSQR_OK;
+  BatchState *B = ctx->batch;
+  if (kVariants[v].lpr == 0) *ok = B->lines_sorted;
+  if (kVariants[v].lpr < 0) {
+    int rc;
+    if ((rc = batch_units(ctx))) return rc;
+    *ok = B->units_ok;
+  }
+  return PLSQR_OK;
+}
+
+unsigned batched_check_word(bool reset) { return plsqr::check_word(reset); }
+
 // ---- variant choice ---------------------------------------------------------
 static int time_product(plsqr_ctx *ctx, BatchState *B, LaunchFn f, int mode, int reps,
                         double *ms) {
@@ -406,10 +505,20 @@ static int batch_choose(plsqr_ctx *ctx, int want_rows, int want_cols) {
     }
   }
   int rc;
+  // a choice this operator cannot run (a cached one, made on another
+  // operator of the same shape) is timed again; the units form's layouts are
+  // built here, outside any graph capture
+  for (int *v : {&vr, &vc}) {
+    bool ok = false;
+    if (*v >= 0 && (rc = variant_usable(ctx, *v, B->kw, &ok))) return rc;
+    if (!ok) *v = -1;
+  }
   double best_r = 1e30, best_c = 1e30;
   if (vr < 0 || vc < 0) {
     for (int v = 0; v < kNumVariants; ++v) {
-      if (!variant_ok(v, B->kw) || (kVariants[v].lpr == 0 && !B->lines_sorted)) continue;
+      bool ok = false;
+      if ((rc = variant_usable(ctx, v, B->kw, &ok))) return rc;
+      if (!ok) continue;
       double t;
       if (vr < 0) {
         if ((rc = time_product(ctx, B, kVariants[v].rows, kScaleOne, 3, &t))) return rc;
@@ -547,10 +656,15 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
   CK(cudaSetDevice(ctx->opts.device));
   if ((rc = batch_prepare(ctx, kw))) return rc;
   BatchState *B = ctx->batch;
-  if (!B->lines_sorted && ((a->variant_rows >= 0 && kVariants[a->variant_rows].lpr == 0) ||
-                           (a->variant_cols >= 0 && kVariants[a->variant_cols].lpr == 0))) {
-    ctx_set_error(ctx, "the slab form needs every kernel row and column in ascending order");
-    return PLSQR_ERR_ARG;
+  for (const int v : {a->variant_rows, a->variant_cols}) {
+    bool ok = true;
+    if (v >= 0 && (rc = variant_usable(ctx, v, kw, &ok))) return rc;
+    if (!ok) {
+      ctx_set_error(ctx, "product variant %d cannot run on this operator (the slab form needs "
+                         "every kernel row and column in ascending order, the units form "
+                         "slabs of %d rows fitting 16-bit indices)", v, kBUnitSlab);
+      return PLSQR_ERR_ARG;
+    }
   }
   B->k = k;
   B->kw = kw;
@@ -621,8 +735,12 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
       B->kw = kq;
       B->k = std::min(k, kq);
       // the caller's variants where they suit the narrower block
-      const int vr = variant_ok(a->variant_rows, kq) ? a->variant_rows : -1;
-      const int vc = variant_ok(a->variant_cols, kq) ? a->variant_cols : -1;
+      bool okr = false, okc = false;
+      if ((rc = variant_usable(ctx, a->variant_rows, kq, &okr)) ||
+          (rc = variant_usable(ctx, a->variant_cols, kq, &okc)))
+        return rc;
+      const int vr = okr ? a->variant_rows : -1;
+      const int vc = okc ? a->variant_cols : -1;
       if ((rc = batch_choose(ctx, vr, vc))) return rc;
       width_var[kq] = std::make_pair(B->var_rows, B->var_cols);
     }
@@ -862,7 +980,9 @@ extern "C" int plsqr_batch_bench_aprod(plsqr_ctx *ctx, int32_t k, int mode, int3
     if ((rc = batch_choose(ctx, -1, -1))) return rc;
     variant = mode == 1 ? B->var_rows : B->var_cols;
   }
-  if (kVariants[variant].lpr == 0 && !B->lines_sorted) return PLSQR_ERR_ARG;
+  bool ok = false;
+  if ((rc = variant_usable(ctx, variant, kw, &ok))) return rc;
+  if (!ok) return PLSQR_ERR_ARG;
   const Variant &V = kVariants[variant];
   return time_product(ctx, B, mode == 1 ? V.rows : V.cols, kScaleOne, reps, ms_per_launch);
 }

@@ -603,10 +603,12 @@ int plsqr_check_flags(int32_t *checked, uint32_t *flags, int32_t reset) {
 #else
   *checked = 0;
 #endif
-  // the unit kernels run in this translation unit, their fill and reorder in slab.cu
-  const unsigned a = plsqr::check_word(reset != 0), b = slab_check_word(reset != 0);
-  if (a == ~0u || b == ~0u) return PLSQR_ERR_CUDA;
-  *flags = a | b;
+  // the unit kernels run in this translation unit, their fill and reorder in
+  // slab.cu, the batched solver's k-wide unit kernels in batched.cu
+  const unsigned a = plsqr::check_word(reset != 0), b = slab_check_word(reset != 0),
+                 c = batched_check_word(reset != 0);
+  if (a == ~0u || b == ~0u || c == ~0u) return PLSQR_ERR_CUDA;
+  *flags = a | b | c;
   return PLSQR_OK;
 }
 

@@ -136,14 +136,15 @@ int slab_dyn_blocks(const plsqr_ctx *ctx, bool fp32);
 int slab_plan(plsqr_ctx *ctx);
 template <typename T>
 int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
-                DevUnitsT<T> *out, bool hilo = false);
+                DevUnitsT<T> *out, bool hilo = false, bool lane_lines = false);
 // slabs of `slab` entries over an index space of n_idx: few enough for the
 // build, 16-bit indices, and the slab and summing area of 1,024 threads in
 // shared memory
 template <typename T>
 bool units_fit(int32_t n_idx, int32_t slab, bool hilo = false);
-// slab.cu: the bounds-check word of its kernels (check.cuh)
+// slab.cu / batched.cu: the bounds-check words of their kernels (check.cuh)
 unsigned slab_check_word(bool reset);
+unsigned batched_check_word(bool reset);
 // plsqr_gpu.cu: unit product launch and its shared-memory attribute
 // x_lo (FP32 layouts built with hilo): the low halves of the pairs x + x_lo
 template <typename T>

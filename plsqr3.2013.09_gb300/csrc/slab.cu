@@ -136,9 +136,14 @@ template int build_slab<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t, 
 // The unit layout (units.cuh) of a by-line matrix: segments counted as for
 // the slab layout, lines of each slab sorted longest segment first and cut
 // into units of kUnitLines, every unit's groups assigned to 32 lanes.
+//
+// lane_lines: lane j of a unit streams line j alone (q = the unit's longest
+// segment in groups, the shorter ones padded with zero entries), for the
+// k-wide products of the batched solver, whose lanes then need no summing
+// across lanes.
 template <typename T>
 int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
-                DevUnitsT<T> *out, bool hilo) {
+                DevUnitsT<T> *out, bool hilo, bool lane_lines) {
   const int n_lines = L.n_lines;
   const int n_slabs = std::max(1, (n_idx + slab - 1) / slab);
   if (n_slabs > kMaxSlabs) return PLSQR_ERR_ARG;
@@ -163,7 +168,7 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   // line slots stay empty) for shorter units and a shorter launch tail
   int lpu = kUnitLines;
   if (const char *e = getenv("PLSQR_UNIT_LINES"))
-    if (atoi(e) >= 1 && atoi(e) <= kUnitLines) lpu = atoi(e);
+    if (atoi(e) >= 1 && atoi(e) <= kUnitLines && !lane_lines) lpu = atoi(e);
   for (int s = 0; s < n_slabs; ++s) {
     const int64_t *cs = hc.data() + (size_t)s * n_lines;
     for (int l = 0; l < n_lines; ++l) ord[(size_t)l] = l;
@@ -171,9 +176,12 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
     ubeg[(size_t)s] = (int32_t)uq.size();
     for (int i0 = 0; i0 < n_lines; i0 += lpu) {
       const int u = (int)uq.size();
-      int64_t run = 0;
+      int64_t run = 0, qmax = 0;
+      if (lane_lines)
+        for (int i = 0; i < lpu && i0 + i < n_lines; ++i)
+          qmax = std::max<int64_t>(qmax, cs[ord[(size_t)i0 + i]] / 8);
       for (int i = 0; i < kUnitLines; ++i) {
-        uc.push_back((int32_t)run);
+        uc.push_back((int32_t)(lane_lines ? i * qmax : run));
         if (i < lpu && i0 + i < n_lines) {
           const int l = ord[(size_t)i0 + i];
           uline.push_back(l);
@@ -184,9 +192,10 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
           uline.push_back(-1);
         }
       }
+      if (lane_lines) run = kUnitLines * qmax;
       uc.push_back((int32_t)run);
       if (run > INT32_MAX / 2) return PLSQR_ERR_ARG;
-      const int64_t q = (run + 31) / 32;
+      const int64_t q = lane_lines ? qmax : (run + 31) / 32;
       uq.push_back((int32_t)q);
       uslot.push_back(slots);
       slots += 32 * q;
@@ -232,13 +241,18 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   // default for the FP32 hi + lo pairs (inner iteration 2.62 -> 2.56 ms on
   // the 96x96x32 problem), not for FP64 (measured no change) nor the FP32
   // mirror alone; PLSQR_UNIT_BANKS=0/1 overrides.
-  bool banks = sizeof(T) == 4 && hilo;
+  // The lane-per-line layout of the batched k-wide products gathers 16-byte
+  // pieces of rows staged piece-major: 32 lanes over 8 groups of 4 banks
+  // (row mod 8); ordered by default (on the 48x48x32 problem 10.4 shared-
+  // memory wavefronts per gather unordered, against 4 at best).
+  bool banks = (sizeof(T) == 4 && hilo) || lane_lines;
   if (const char *e = getenv("PLSQR_UNIT_BANKS")) banks = atoi(e) == 1;
   if (banks) {
-    const int wave = (sizeof(T) == 8 || hilo) ? 16 : 32;
+    const int wave = lane_lines ? 32 : (sizeof(T) == 8 || hilo) ? 16 : 32;
+    const int groups = lane_lines ? 8 : wave;
     const int nu = (int)uq.size();
-    k_units_banks<<<std::max(1, (nu + 3) / 4), 128, 0, ctx->stream>>>(U, nu, wave, out->idx,
-                                                                     out->val);
+    k_units_banks<<<std::max(1, (nu + 3) / 4), 128, 0, ctx->stream>>>(U, nu, wave, groups,
+                                                                     out->idx, out->val);
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(ctx->stream));
@@ -275,9 +289,9 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   return PLSQR_OK;
 }
 template int build_units<double>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
-                                 DevUnitsT<double> *, bool);
+                                 DevUnitsT<double> *, bool, bool);
 template int build_units<float>(plsqr_ctx *, const DevLines &, int32_t, int32_t,
-                                DevUnitsT<float> *, bool);
+                                DevUnitsT<float> *, bool, bool);
 
 template <typename T>
 bool units_fit(int32_t n_idx, int32_t slab, bool hilo) {

@@ -108,12 +108,13 @@ __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__r
 // lane's group; the entries of a group may come in any order (they are
 // summed into the lane's line either way).  Greedy, a warp per unit and a
 // thread per step: for e = 0..7, lane by lane, the lane's remaining entry
-// whose bank the wavefront has used least so far.
+// whose bank the wavefront has used least so far.  banks: the bank groups an
+// entry's gather can fall in (index mod banks): lanes_per_wave for 4- and
+// 8-byte gathers, 8 for the 16-byte pieces of the batched k-wide products.
 template <typename T>
-__global__ void k_units_banks(UnitsArgs<T> U, int n_units, int lanes_per_wave,
+__global__ void k_units_banks(UnitsArgs<T> U, int n_units, int lanes_per_wave, int banks,
                               uint16_t *__restrict__ sidx, T *__restrict__ sval) {
   constexpr int E = UnitPieces<T>::E, P = UnitPieces<T>::P;
-  const int banks = lanes_per_wave;  // bank groups one entry occupies: 32 / entry words
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
   for (int u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < n_units; u += warps) {

@@ -89,7 +89,8 @@ def test_every_variant_gives_the_same_iterates(pkg, grid32, k):
             vw, lpr, u = pkg._native.batch_variant(v)
         except pkg._native.PlsqrError:
             break
-        if lpr == 0 or (kw % vw == 0 and kw // vw <= lpr):  # lpr 0: slab form
+        # lpr 0: slab form; lpr -1: units form (blocks of 4 or 8)
+        if lpr == 0 or (lpr < 0 and kw <= 8) or (lpr > 0 and kw % vw == 0 and kw // vw <= lpr):
             ok.append(v)
     assert len(ok) >= 7
     with pkg.Context(prob) as ctx:
@@ -148,6 +149,9 @@ def test_batch_arguments_are_checked(pkg, grid32):
         narrow = [v for v in range(13) if pkg._native.batch_variant(v) == (2, 8, 2)]
         with pytest.raises(pkg._native.PlsqrError):
             ctx.batch_lsqr(np.zeros((32, prob.m_k)), variant_rows=narrow[0])
+        # the units form takes blocks of 4 or 8 only
+        with pytest.raises(pkg._native.PlsqrError):
+            ctx.batch_lsqr(np.zeros((16, prob.m_k)), variant_rows=units_variant(pkg))
 
 
 def test_damping_weight_round_trip(pkg, problems):
@@ -189,6 +193,46 @@ def test_warm_start_and_cold_fallback(pkg, grid32):
     # the far start fell back: the same bits as the cold solve
     assert np.array_equal(back["x"][1], cold["x"][1])
     assert np.array_equal(back["x"][0], warm["x"][0])
+
+
+def units_variant(pkg):
+    for v in range(64):
+        try:
+            if pkg._native.batch_variant(v)[1] < 0:
+                return v
+        except pkg._native.PlsqrError:
+            break
+    raise AssertionError("no units form among the product variants")
+
+
+@pytest.mark.parametrize("k", [3, 8])
+def test_units_form_matches_team_form(pkg, grid32, k):
+    """The units form (FP32 unit layout, the block's rows staged per slab in
+    shared memory) gives the team form's iterates to FP32 accuracy, reaches
+    the FP64 solutions, and a right-hand side gives the same bits alone and
+    inside a block of the same width."""
+    prob, insts = grid32
+    sel = pkg.batch.pick(insts, k)
+    b = np.stack([i.b_k for i in sel])
+    lam = [i.lam for i in sel]
+    vu = units_variant(pkg)
+    xstar = np.stack([fp64_solution(pkg, prob, i, 800)["x"] for i in sel])
+    with pkg.Context(prob) as ctx:
+        team = ctx.batch_lsqr(b, lam=lam, sweeps=1, inner=6, variant_rows=1, variant_cols=1)
+        unit = ctx.batch_lsqr(b, lam=lam, sweeps=1, inner=6, variant_rows=vu, variant_cols=vu)
+        assert unit["info"]["variant_rows"] == vu and unit["info"]["variant_cols"] == vu
+        for f in ("alpha", "beta", "rnorm"):
+            assert np.allclose(unit["hist"][f], team["hist"][f], rtol=2e-5, atol=0), f
+        assert rel(unit["x"], team["x"]) <= 1e-4
+        full = ctx.batch_lsqr(b, lam=lam, x_ref=xstar, sweeps=5, inner=60, variant_rows=vu,
+                              variant_cols=vu)
+        for j in range(k):
+            assert rel(full["x"][j], xstar[j]) <= 1e-6, sel[j].name
+        if k == 3:  # width 4 either way: the first right-hand side alone
+            one = ctx.batch_lsqr(b[:1], lam=lam[:1], sweeps=1, inner=6, variant_rows=vu,
+                                 variant_cols=vu)
+            assert np.array_equal(one["x"][0], unit["x"][0])
+            assert np.array_equal(one["hist"][0], unit["hist"][0])
 
 
 def first_at_or_below(err, tol, start=1):

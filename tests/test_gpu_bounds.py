@@ -3,8 +3,9 @@ kernels check every slot, gather index, line and lane they touch, record a
 failed check and skip the access.  A child process loads that build
 (PLSQR_LIB), runs the FP64 and mixed-precision products and solves on
 problems shaped for the layout's edge cases, under the launch shapes the
-switches select, and reads the flags: no check may fail, and the results
-match the normal build's to the usual bars."""
+switches select, and the batched solver's k-wide unit products on blocks of
+4 and 8, and reads the flags: no check may fail and every result is
+finite."""
 from __future__ import annotations
 
 import json
@@ -37,6 +38,7 @@ envs = [{}, {"PLSQR_SLAB_SIZE": "1024", "PLSQR_UNIT_SIZE_F": "1024"},
         {"PLSQR_UNIT_THREADS": "512", "PLSQR_SLAB_SIZE": "12288", "PLSQR_UNIT_SIZE_F": "12288"},
         {"PLSQR_UNIT_LINES": "8", "PLSQR_UNIT_BANKS": "1"}]
 out = {"checked": checked, "runs": []}
+vu = next(v for v in range(64) if N.batch_variant(v)[1] < 0)
 rng = np.random.default_rng(1)
 for env in envs:
     for k in ("PLSQR_SLAB_SIZE", "PLSQR_UNIT_SIZE_F", "PLSQR_UNIT_THREADS", "PLSQR_UNIT_LINES",
@@ -51,6 +53,12 @@ for env in envs:
             c.aprod_host(2, yk, yd, x)
         with pkg.Context(p, precision="mixed") as cm:
             xm = cm.lsqr(sweeps=1, inner=30)["x"]
+        # the batched solver's units form, blocks of 4 and 8
+        with pkg.Context(p) as cb:
+            for kk in (3, 8):
+                bb = np.stack([p.b_k * (1.0 + 0.1 * t) for t in range(kk)])
+                xb = cb.batch_lsqr(bb, sweeps=1, inner=10, variant_rows=vu, variant_cols=vu)["x"]
+                x = np.concatenate([x, xb.ravel()])
         out["runs"].append({"env": env, "case": name, "flags": N.check_flags(reset=True)[1],
                             "finite": bool(np.all(np.isfinite(x64)) and np.all(np.isfinite(xm))
                                            and np.all(np.isfinite(yk)) and np.all(np.isfinite(x)))})
