@@ -232,6 +232,8 @@ def main() -> int:
                     help="batched product variant of A x (-1: pick by timing)")
     ap.add_argument("--variant-cols", type=int, default=-1,
                     help="batched product variant of A^T y (-1: pick by timing)")
+    ap.add_argument("--rhs", type=int, default=32,
+                    help="batched profiling run: right-hand sides (the first of the 32)")
     args = ap.parse_args()
 
     ws, rank, local = dist()
@@ -282,11 +284,11 @@ def main() -> int:
     if args.profile and args.extension == "batched":
         prob = pkg.generate(args.config)
         with pkg.Context(prob, device=local) as ctx:
-            insts = pkg.batch.instances(ctx, prob, args.config)
+            insts = pkg.batch.instances(ctx, prob, args.config)[:args.rhs]
             out = ctx.batch_lsqr(np.stack([i.b_k for i in insts]), lam=[i.lam for i in insts],
                                  sweeps=1, inner=2, variant_rows=args.variant_rows,
                                  variant_cols=args.variant_cols)
-        log(f"profile run: {args.config}, 32 right-hand sides, variants {out['info']}")
+        log(f"profile run: {args.config}, {len(insts)} right-hand sides, variants {out['info']}")
         return 0
     if args.profile and args.extension == "uneven":
         probs = [pkg.generate(c) for c in pkg.multi.uneven_configs()]
