@@ -242,13 +242,14 @@ int build_units(plsqr_ctx *ctx, const DevLines &L, int32_t n_idx, int32_t slab,
   // the 96x96x32 problem), not for FP64 (measured no change) nor the FP32
   // mirror alone; PLSQR_UNIT_BANKS=0/1 overrides.
   // The lane-per-line layout of the batched k-wide products gathers 16-byte
-  // pieces of rows staged piece-major: 32 lanes over 8 groups of 4 banks
-  // (row mod 8); ordered by default (on the 48x48x32 problem 10.4 shared-
-  // memory wavefronts per gather unordered, against 4 at best).
+  // pieces of rows staged piece-major: a wavefront serves 8 lanes, over 8
+  // groups of 4 banks (row mod 8); ordered by default (on the 48x48x32
+  // problem 10.4 shared-memory wavefronts per gather unordered, 7.5 with the
+  // 32 lanes balanced as one wave, against 4 at best).
   bool banks = (sizeof(T) == 4 && hilo) || lane_lines;
   if (const char *e = getenv("PLSQR_UNIT_BANKS")) banks = atoi(e) == 1;
   if (banks) {
-    const int wave = lane_lines ? 32 : (sizeof(T) == 8 || hilo) ? 16 : 32;
+    const int wave = lane_lines ? 8 : (sizeof(T) == 8 || hilo) ? 16 : 32;
     const int groups = lane_lines ? 8 : wave;
     const int nu = (int)uq.size();
     k_units_banks<<<std::max(1, (nu + 3) / 4), 128, 0, ctx->stream>>>(U, nu, wave, groups,
