@@ -101,6 +101,73 @@ __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__r
 // SM on slabs of half that.
 // Each lane prefetches its loads of a later step into L2 (by default all
 // of the next step's).
+// Exact order of one wave of 8 lanes over 8 bank groups: lane j's entry w,
+// of bank group g[j][w], is gathered in round rd[j][w], a lane's rounds all
+// distinct, and a bank group with d entries in the wave used at most
+// ceil(d / 8) times a round, the fewest possible.  A proper 8-edge-colouring
+// of the bipartite multigraph lanes x virtual groups (a group's entries cut
+// into virtual groups of 8, so that no vertex has more than 8 edges), built
+// edge by edge: colour a free at the lane, b free at the group; where a is
+// taken at the group, the path from the group alternating a and b has its
+// colours swapped first (Konig's construction; the path cannot reach the
+// lane, so a is then free at both ends).  Returns false, leaving the
+// caller's greedy order, if a path or a search runs past its bound (a path
+// has at most the wave's 64 edges).
+__host__ __device__ inline bool colour_wave(const unsigned char (&g)[8][8], unsigned char (&rd)[8][8]) {
+  constexpr unsigned char kNone = 0xff;
+  unsigned char vid[8][8], seen[8], at_l[8][8], at_v[64][8], path[64];
+  for (int q = 0; q < 8; ++q) seen[q] = 0;
+  for (int j = 0; j < 8; ++j)
+    for (int w = 0; w < 8; ++w) {
+      const int q = g[j][w] & 7;
+      vid[j][w] = (unsigned char)(q * 8 + seen[q]++ / 8);
+    }
+  for (int j = 0; j < 8; ++j)
+    for (int c = 0; c < 8; ++c) at_l[j][c] = kNone;
+  for (int v = 0; v < 64; ++v)
+    for (int c = 0; c < 8; ++c) at_v[v][c] = kNone;
+  for (int j = 0; j < 8; ++j)
+    for (int w = 0; w < 8; ++w) {
+      const int v = vid[j][w];
+      int a = 0, b = 0;
+      while (a < 8 && at_l[j][a] != kNone) ++a;
+      while (b < 8 && at_v[v][b] != kNone) ++b;
+      if (a == 8 || b == 8) return false;
+      if (at_v[v][a] != kNone) {
+        int len = 0, x = v, col = a;
+        bool at_group = true;
+        for (;;) {
+          const unsigned char e = at_group ? at_v[x][col] : at_l[x][col];
+          if (e == kNone) break;
+          if (len == 64) return false;
+          path[len++] = e;
+          x = at_group ? e / 8 : vid[e / 8][e % 8];
+          at_group = !at_group;
+          col = col == a ? b : a;
+        }
+        for (int i = 0; i < len; ++i) {  // the path's edges leave their colours
+          const int e = path[i], c = (i & 1) ? b : a;
+          at_l[e / 8][c] = kNone;
+          at_v[vid[e / 8][e % 8]][c] = kNone;
+        }
+        for (int i = 0; i < len; ++i) {  // and take the other one
+          const int e = path[i], c = (i & 1) ? a : b;
+          at_l[e / 8][c] = (unsigned char)e;
+          at_v[vid[e / 8][e % 8]][c] = (unsigned char)e;
+        }
+      }
+      at_l[j][a] = (unsigned char)(j * 8 + w);
+      at_v[v][a] = (unsigned char)(j * 8 + w);
+    }
+  for (int j = 0; j < 8; ++j)
+    for (int c = 0; c < 8; ++c) {
+      const int e = at_l[j][c];
+      if (e == kNone || e / 8 != j) return false;
+      rd[j][e % 8] = (unsigned char)c;
+    }
+  return true;
+}
+
 // Setup, optional: order each lane's 8 entries of every step so that the
 // lanes one shared-memory wavefront serves (16 for 8-byte entries: FP64, or
 // FP32 hi + lo pairs; 32 for 4-byte ones) gather from distinct banks where
@@ -110,7 +177,9 @@ __global__ void k_units_fill(const int64_t *__restrict__ ptr, const int32_t *__r
 // thread per step: for e = 0..7, lane by lane, the lane's remaining entry
 // whose bank the wavefront has used least so far.  banks: the bank groups an
 // entry's gather can fall in (index mod banks): lanes_per_wave for 4- and
-// 8-byte gathers, 8 for the 16-byte pieces of the batched k-wide products.
+// 8-byte gathers, 8 for the 16-byte pieces of the batched k-wide products,
+// whose waves of 8 lanes over 8 bank groups take the exact order of
+// colour_wave instead.
 template <typename T>
 __global__ void k_units_banks(UnitsArgs<T> U, int n_units, int lanes_per_wave, int banks,
                               uint16_t *__restrict__ sidx, T *__restrict__ sval) {
@@ -131,6 +200,20 @@ __global__ void k_units_banks(UnitsArgs<T> U, int n_units, int lanes_per_wave, i
           for (int w = 0; w < 8; ++w) {
             id[j][w] = sidx[(base + (int64_t)k * 32 + h + j) * 8 + w];
             v[j][w] = sval[(base * P + ((int64_t)k * P + w / E) * 32 + h + j) * E + w % E];
+          }
+        }
+        if (lanes_per_wave == 8 && banks == 8) {
+          unsigned char gq[8][8], rd[8][8];
+          for (int j = 0; j < 8; ++j)
+            for (int w = 0; w < 8; ++w) gq[j][w] = (unsigned char)(id[j][w] & 7);
+          if (colour_wave(gq, rd)) {
+            for (int j = 0; j < 8; ++j)
+              for (int w = 0; w < 8; ++w) {
+                const int e = rd[j][w];
+                sidx[(base + (int64_t)k * 32 + h + j) * 8 + e] = id[j][w];
+                sval[(base * P + ((int64_t)k * P + e / E) * 32 + h + j) * E + e % E] = v[j][w];
+              }
+            continue;
           }
         }
         for (int e = 0; e < 8; ++e) {
