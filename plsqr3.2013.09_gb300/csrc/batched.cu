@@ -7,11 +7,15 @@
 //     DX = LSQR(A_hi, R), `inner` iterations, one k-wide product per matrix read
 //     X += DX
 //
-// where A_j = [K; lambda_j D].  The inner iteration is four kernels captured
+// where A_j = [K; lambda_j D].  The inner iteration is four steps captured
 // as one CUDA graph: A x, scaling of u, A^T y, scaling of v with the x/w update
-// and the scalar tail.  The product variant (gather width, lanes per line,
-// nonzeros in flight) of each direction is picked by timing the candidates on
-// the operator and cached per (line-length histogram, block width).
+// and the scalar tail.  The product variant of each direction (the team form:
+// gather width, lanes per line, nonzeros in flight; the slab form; for blocks
+// of 4 and 8 the units form of kernels_bunits.cuh) is picked by timing the
+// candidates on the operator and cached per (line-length histogram, block
+// width).  With retire_every the host looks at the solves every few
+// iterations, lets the finished ones go and packs the rest into the
+// narrowest block width that holds them.
 #include <cuda_runtime.h>
 #include <stdlib.h>
 #include <string.h>
