@@ -10,8 +10,8 @@
 // where A_j = [K; lambda_j D].  The inner iteration is four steps captured
 // as one CUDA graph: A x, scaling of u, A^T y, scaling of v with the x/w update
 // and the scalar tail.  The product variant of each direction (the team form:
-// gather width, lanes per line, nonzeros in flight; the slab form; for blocks
-// of 4 and 8 the units form of kernels_bunits.cuh) is picked by timing the
+// gather width, lanes per line, nonzeros in flight; the slab form; the units
+// form of kernels_bunits.cuh, in passes of 8 columns) is picked by timing the
 // candidates on the operator and cached per (line-length histogram, block
 // width).  With retire_every the host looks at the solves every few
 // iterations, lets the finished ones go and packs the rest into the
@@ -88,8 +88,8 @@ struct BatchState {
     int g_rows = 0, g_cols = 0;
   };
   std::map<int, SlabPlan> slab;
-  // units form (blocks of 4 or 8): FP32 unit layouts of K by row and by
-  // column, one lane per line, and their k-wide partial sums
+  // units form: FP32 unit layouts of K by row and by column, one lane per
+  // line, and the partial sums of one pass of 4 or 8 columns
   DevUnitsT<float> ur, uc;
   bool units_tried = false, units_ok = false;
   double *upart = nullptr;
@@ -154,25 +154,35 @@ template <int KW>
 size_t bunits_smem(const DevUnitsT<float> &U) {
   return sizeof(float) * KW * (size_t)std::min(U.slab, U.n_idx);
 }
+// Blocks of 4: one pass of 4 columns; wider blocks: passes of 8 columns over
+// the right-hand sides in use (the padding columns past k are left alone),
+// the last pass finishing the product.
 template <int KW>
 void launch_units_rows_t(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
   const DevUnitsT<float> &U = B.ur;
-  cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
-  k_bunits<KW><<<U.blocks, kBUnitThreads, bunits_smem<KW>(U), s>>>(units_args(U), U.next, B.Vf,
-                                                                   B.upart);
-  k_bunits_rows<KW><<<B.gur, kBatchThreads, 0, s>>>(B.upart, U.n_slabs, ctx->m_k, ctx->D.csr(),
-                                                     B.k, B.V, B.U, B.LAM, mode, B.st, B.cf,
-                                                     B.parts);
+  const int last = std::max(0, (B.k - 1) / KW) * KW;
+  for (int c0 = 0; c0 <= last; c0 += KW) {
+    cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
+    k_bunits<KW><<<U.blocks, kBUnitThreads, bunits_smem<KW>(U), s>>>(units_args(U), U.next, B.Vf,
+                                                                     B.kw, c0, B.upart);
+    k_bunits_rows<KW><<<B.gur, kBatchThreads, 0, s>>>(B.upart, U.n_slabs, ctx->m_k, ctx->D.csr(),
+                                                       B.k, B.kw, c0, B.V, B.U, B.LAM, mode, B.st,
+                                                       B.cf, B.parts, c0 == last);
+  }
 }
 template <int KW>
 void launch_units_cols_t(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
   const DevUnitsT<float> &U = B.uc;
-  cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
-  k_bunits<KW><<<U.blocks, kBUnitThreads, bunits_smem<KW>(U), s>>>(units_args(U), U.next, B.Uf,
-                                                                   B.upart);
-  k_bunits_cols<KW><<<B.guc, kBatchThreads, 0, s>>>(B.upart, U.n_slabs, ctx->DC.csr(), ctx->m_k,
-                                                     ctx->n, B.k, B.U, B.V, B.LAM, mode, B.st,
-                                                     B.cf, B.parts);
+  const int last = std::max(0, (B.k - 1) / KW) * KW;
+  for (int c0 = 0; c0 <= last; c0 += KW) {
+    cudaMemsetAsync(U.next, 0, sizeof(int) * U.n_slabs, s);
+    k_bunits<KW><<<U.blocks, kBUnitThreads, bunits_smem<KW>(U), s>>>(units_args(U), U.next, B.Uf,
+                                                                     B.kw, c0, B.upart);
+    k_bunits_cols<KW><<<B.guc, kBatchThreads, 0, s>>>(B.upart, U.n_slabs, ctx->DC.csr(),
+                                                       ctx->m_k, ctx->n, B.k, B.kw, c0, B.U, B.V,
+                                                       B.LAM, mode, B.st, B.cf, B.parts,
+                                                       c0 == last);
+  }
 }
 void launch_units_rows(plsqr_ctx *ctx, const BatchState &B, int mode, cudaStream_t s) {
   if (B.kw == 4) return launch_units_rows_t<4>(ctx, B, mode, s);
@@ -192,7 +202,8 @@ const Variant kVariants[] = {
     VARIANT(4, 32, 2), VARIANT(4, 32, 4), VARIANT(2, 16, 2), VARIANT(2, 16, 4),
     VARIANT(2, 32, 2), VARIANT(2, 32, 4), VARIANT(2, 8, 2),  VARIANT(2, 8, 4),
     Variant{4, 0, 0, launch_slab_rows, launch_slab_cols},
-    // lpr = -1: the units form (kernels_bunits.cuh), blocks of 4 or 8
+    // lpr = -1: the units form (kernels_bunits.cuh): blocks of 4, or passes
+    // of 8 columns
     Variant{4, -1, 0, launch_units_rows, launch_units_cols},
 };
 #undef VARIANT
@@ -202,7 +213,7 @@ bool variant_ok(int v, int kp) {
   if (v < 0 || v >= kNumVariants) return false;
   const Variant &V = kVariants[v];
   if (V.lpr == 0) return true;
-  if (V.lpr < 0) return kp == 4 || kp == 8;
+  if (V.lpr < 0) return kp % 4 == 0 && kp <= kBatchMax;
   return kp % V.vw == 0 && kp / V.vw <= V.lpr;
 }
 
@@ -666,7 +677,7 @@ extern "C" int plsqr_batch_lsqr(plsqr_ctx *ctx, const plsqr_batch_args *a, doubl
     if (!ok) {
       ctx_set_error(ctx, "product variant %d cannot run on this operator (the slab form needs "
                          "every kernel row and column in ascending order, the units form "
-                         "slabs of %d rows fitting 16-bit indices)", v, kBUnitSlab);
+                         "at most 64 slabs of %d rows)", v, kBUnitSlab);
       return PLSQR_ERR_ARG;
     }
   }

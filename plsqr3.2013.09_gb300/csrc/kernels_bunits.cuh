@@ -1,5 +1,6 @@
 // k-wide products of the batched solver on the unit layout (units.cuh, built
-// with lane_lines): blocks of KW = 4 or 8 right-hand sides.
+// with lane_lines): passes over KW = 4 or 8 columns of the block (a block of
+// 16 or 32 right-hand sides in passes of 8).
 //
 // The team form (kernels_batched.cuh) streams the matrix as int32 index +
 // FP32 value (8 bytes a nonzero) and gathers 4*KW bytes of the block's row
@@ -28,8 +29,8 @@ constexpr int kBUnitSlab = 6144;  // rows of the block per slab: 192 KB at KW = 
 
 template <int KW>
 __global__ void __launch_bounds__(kBUnitThreads, 1)
-    k_bunits(UnitsArgs<float> A, int *__restrict__ next, const float *__restrict__ xf,
-             double *__restrict__ partial) {
+    k_bunits(UnitsArgs<float> A, int *__restrict__ next, const float *__restrict__ xf, int kp,
+             int col0, double *__restrict__ partial) {
   static_assert(KW == 4 || KW == 8, "blocks of 4 or 8 right-hand sides");
   constexpr int V4 = KW / 4;  // float4 pieces of a row
   constexpr int P = UnitPieces<float>::P;
@@ -49,12 +50,13 @@ __global__ void __launch_bounds__(kBUnitThreads, 1)
     if (!left) continue;
     const int64_t xbase = (int64_t)s * A.slab;
     const int len = (int)min((int64_t)A.slab, (int64_t)A.n_idx - xbase);
-    // piece t of row r at xs4[t * plane + r]: a wavefront's random rows then
-    // spread over all 8 groups of 4 banks (rows of 32 bytes side by side
-    // would start on only 4 of them)
-    const float4 *src = reinterpret_cast<const float4 *>(xf) + xbase * V4;
+    // columns col0 .. col0 + KW - 1 of the block xf[n_idx][kp]; piece t of
+    // row r at xs4[t * plane + r]: a wavefront's random rows then spread over
+    // all 8 groups of 4 banks (rows of 32 bytes side by side would start on
+    // only 4 of them)
+    const float4 *src = reinterpret_cast<const float4 *>(xf + xbase * kp + col0);
     for (int i = threadIdx.x; i < len * V4; i += kBUnitThreads)
-      xs4[(i % V4) * plane + i / V4] = __ldg(src + i);
+      xs4[(i % V4) * plane + i / V4] = __ldg(src + (int64_t)(i / V4) * (kp / 4) + i % V4);
     __syncthreads();
     double *part = partial + (int64_t)s * A.n_lines * KW;
     for (;;) {
@@ -114,60 +116,65 @@ __global__ void __launch_bounds__(kBUnitThreads, 1)
   }
 }
 
-// A x of the units form: U_k[r][j] = s_j U_k[r][j] + the sum of
-// partial[s][r][j] over the slabs in slab order, and the damping rows
-// U_d[r][j] = s_j U_d[r][j] + lambda_j (D V)[r][j] in FP64, in one grid-stride
-// pass; the last block forms beta_j (rows_finish).
+// A x of the units form, columns col0 .. col0 + KW - 1 of the block
+// u[m][kp]: U_k[r][j] = s_j U_k[r][j] + the sum of partial[s][r][j - col0]
+// over the slabs in slab order, and the damping rows U_d[r][j] = s_j
+// U_d[r][j] + lambda_j (D V)[r][j] in FP64, in one grid-stride pass; sums of
+// squares to parts[block * kp + j]; with `finish` (the block's last pass) the
+// last block forms every beta_j (rows_finish).
 template <int KW>
 __global__ void __launch_bounds__(kBatchThreads)
-    k_bunits_rows(const double *__restrict__ partial, int n_slabs, int m_k, Csr D, int k,
-                  const double *__restrict__ v64, double *__restrict__ u,
+    k_bunits_rows(const double *__restrict__ partial, int n_slabs, int m_k, Csr D, int k, int kp,
+                  int col0, const double *__restrict__ v64, double *__restrict__ u,
                   const double *__restrict__ lambda, int mode, DevState *__restrict__ st,
-                  BatchCoef *__restrict__ cf, double *__restrict__ parts) {
+                  BatchCoef *__restrict__ cf, double *__restrict__ parts, int finish) {
   __shared__ double red[kBatchThreads];
   // each thread keeps one right-hand side: the block and the grid stride
   // are multiples of KW
-  const int j = threadIdx.x & (KW - 1);
+  const int j = col0 + (threadIdx.x & (KW - 1));
   const double sc = (j < k && mode == kScaleNegAlpha) ? -st[j].alpha : 1.0;
   const double lam = (j < k && lambda) ? lambda[j] : 1.0;
   const int64_t tk = (int64_t)m_k * KW, total = tk + (int64_t)D.n_lines * KW;
   double sq = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)kBatchThreads + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * kBatchThreads) {
+    const int64_t r = i / KW;  // a row of [K; D]
     double a;
     if (i < tk) {
       a = 0.0;
       for (int sl = 0; sl < n_slabs; ++sl) a += __ldcs(partial + (int64_t)sl * tk + i);
     } else {
-      const int64_t r = (i - tk) / KW;
       double t = 0.0;
-      for (int64_t e = D.ptr[r]; e < D.ptr[r + 1]; ++e)
-        t = fma(D.val[e], v64[(int64_t)D.idx[e] * KW + j], t);
+      for (int64_t e = D.ptr[r - m_k]; e < D.ptr[r - m_k + 1]; ++e)
+        t = fma(D.val[e], v64[(int64_t)D.idx[e] * kp + j], t);
       a = dmul(lam, t);
     }
     if (j < k) {
-      const double y = dadd(dmul(sc, u[i]), a);
-      u[i] = y;
+      double *p = u + r * kp + j;
+      const double y = dadd(dmul(sc, *p), a);
+      *p = y;
       sq = fma(y, y, sq);
     }
   }
   const double b = batch_block_sum(sq, KW, red);
-  if ((int)threadIdx.x < KW) parts[(int64_t)blockIdx.x * KW + threadIdx.x] = b;
-  if (!batch_last_block(&cf->count)) return;
-  rows_finish(parts, gridDim.x, KW, k, mode, st, cf);
+  if ((int)threadIdx.x < KW) parts[(int64_t)blockIdx.x * kp + col0 + threadIdx.x] = b;
+  if (!finish || !batch_last_block(&cf->count)) return;
+  rows_finish(parts, gridDim.x, kp, k, mode, st, cf);
 }
 
-// A^T y of the units form: V[c][j] = s_j V[c][j] + (the slabs' partials in
-// slab order) + lambda_j (D^T U_d)[c][j], FP64; the last block finishes the
+// A^T y of the units form, columns col0 .. col0 + KW - 1 of the block
+// v[n][kp]: V[c][j] = s_j V[c][j] + (the slabs' partials in slab order) +
+// lambda_j (D^T U_d)[c][j], FP64; with `finish` the last block finishes the
 // product (cols_finish), as k_bslab_cols does.
 template <int KW>
 __global__ void __launch_bounds__(kBatchThreads)
     k_bunits_cols(const double *__restrict__ partial, int n_slabs, Csr DC, int m_k, int n,
-                  int k, const double *__restrict__ u64, double *__restrict__ v,
-                  const double *__restrict__ lambda, int mode, DevState *__restrict__ st,
-                  BatchCoef *__restrict__ cf, double *__restrict__ parts) {
+                  int k, int kp, int col0, const double *__restrict__ u64,
+                  double *__restrict__ v, const double *__restrict__ lambda, int mode,
+                  DevState *__restrict__ st, BatchCoef *__restrict__ cf,
+                  double *__restrict__ parts, int finish) {
   __shared__ double red[kBatchThreads];
-  const int j = threadIdx.x & (KW - 1);
+  const int j = col0 + (threadIdx.x & (KW - 1));
   double sc = 1.0;
   bool act = j < k;
   if (act && (mode == kScaleNegBeta || mode == kScaleZero)) {
@@ -175,7 +182,7 @@ __global__ void __launch_bounds__(kBatchThreads)
     sc = mode == kScaleZero ? 0.0 : -st[j].beta;
   }
   const double lam = (j < k && lambda) ? lambda[j] : 1.0;
-  const double *ud = u64 + (int64_t)m_k * KW;
+  const double *ud = u64 + (int64_t)m_k * kp;
   const int64_t total = (int64_t)n * KW;
   double sq = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)kBatchThreads + threadIdx.x; i < total;
@@ -185,17 +192,18 @@ __global__ void __launch_bounds__(kBatchThreads)
     for (int sl = 0; sl < n_slabs; ++sl) a += __ldcs(partial + (int64_t)sl * total + i);
     double d = 0.0;
     for (int64_t e = DC.ptr[c]; e < DC.ptr[c + 1]; ++e)
-      d = fma(DC.val[e], ud[(int64_t)DC.idx[e] * KW + j], d);
+      d = fma(DC.val[e], ud[(int64_t)DC.idx[e] * kp + j], d);
     if (act) {
-      const double y = dadd(dmul(sc, v[i]), dadd(a, dmul(lam, d)));
-      v[i] = y;
+      double *p = v + c * kp + j;
+      const double y = dadd(dmul(sc, *p), dadd(a, dmul(lam, d)));
+      *p = y;
       sq = fma(y, y, sq);
     }
   }
   const double b = batch_block_sum(sq, KW, red);
-  if ((int)threadIdx.x < KW) parts[(int64_t)blockIdx.x * KW + threadIdx.x] = b;
-  if (!batch_last_block(&cf->count)) return;
-  cols_finish(parts, gridDim.x, KW, k, mode, st, cf);
+  if ((int)threadIdx.x < KW) parts[(int64_t)blockIdx.x * kp + col0 + threadIdx.x] = b;
+  if (!finish || !batch_last_block(&cf->count)) return;
+  cols_finish(parts, gridDim.x, kp, k, mode, st, cf);
 }
 
 }  // namespace plsqr

@@ -89,8 +89,8 @@ def test_every_variant_gives_the_same_iterates(pkg, grid32, k):
             vw, lpr, u = pkg._native.batch_variant(v)
         except pkg._native.PlsqrError:
             break
-        # lpr 0: slab form; lpr -1: units form (blocks of 4 or 8)
-        if lpr == 0 or (lpr < 0 and kw <= 8) or (lpr > 0 and kw % vw == 0 and kw // vw <= lpr):
+        # lpr 0: slab form; lpr -1: units form (passes of 4 or 8 columns)
+        if lpr <= 0 or (kw % vw == 0 and kw // vw <= lpr):
             ok.append(v)
     assert len(ok) >= 7
     with pkg.Context(prob) as ctx:
@@ -149,9 +149,6 @@ def test_batch_arguments_are_checked(pkg, grid32):
         narrow = [v for v in range(13) if pkg._native.batch_variant(v) == (2, 8, 2)]
         with pytest.raises(pkg._native.PlsqrError):
             ctx.batch_lsqr(np.zeros((32, prob.m_k)), variant_rows=narrow[0])
-        # the units form takes blocks of 4 or 8 only
-        with pytest.raises(pkg._native.PlsqrError):
-            ctx.batch_lsqr(np.zeros((16, prob.m_k)), variant_rows=units_variant(pkg))
 
 
 def test_damping_weight_round_trip(pkg, problems):
@@ -205,11 +202,12 @@ def units_variant(pkg):
     raise AssertionError("no units form among the product variants")
 
 
-@pytest.mark.parametrize("k", [3, 8])
+@pytest.mark.parametrize("k", [3, 8, 20])
 def test_units_form_matches_team_form(pkg, grid32, k):
     """The units form (FP32 unit layout, the block's rows staged per slab in
-    shared memory) gives the team form's iterates to FP32 accuracy, reaches
-    the FP64 solutions, and a right-hand side gives the same bits alone and
+    shared memory; a block of 20 in passes of 8 columns, the last one partly
+    padding) gives the team form's iterates to FP32 accuracy, reaches the
+    FP64 solutions, and a right-hand side gives the same bits alone and
     inside a block of the same width."""
     prob, insts = grid32
     sel = pkg.batch.pick(insts, k)

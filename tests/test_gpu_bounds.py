@@ -4,7 +4,7 @@ failed check and skip the access.  A child process loads that build
 (PLSQR_LIB), runs the FP64 and mixed-precision products and solves on
 problems shaped for the layout's edge cases, under the launch shapes the
 switches select, and the batched solver's k-wide unit products on blocks of
-4 and 8, and reads the flags: no check may fail and every result is
+4, 8 and 32 (passes of 8 columns), and reads the flags: no check may fail and every result is
 finite."""
 from __future__ import annotations
 
@@ -53,9 +53,9 @@ for env in envs:
             c.aprod_host(2, yk, yd, x)
         with pkg.Context(p, precision="mixed") as cm:
             xm = cm.lsqr(sweeps=1, inner=30)["x"]
-        # the batched solver's units form, blocks of 4 and 8
+        # the batched solver's units form: blocks of 4, 8 and 32 (passes of 8)
         with pkg.Context(p) as cb:
-            for kk in (3, 8):
+            for kk in (3, 8, 20):
                 bb = np.stack([p.b_k * (1.0 + 0.1 * t) for t in range(kk)])
                 xb = cb.batch_lsqr(bb, sweeps=1, inner=10, variant_rows=vu, variant_cols=vu)["x"]
                 x = np.concatenate([x, xb.ravel()])
