@@ -339,10 +339,10 @@ void plsqr_default_batch_args(plsqr_batch_args *a);
 /* Product variants: kVW-wide gathers (4 = float4, 2 = float2), kLPR lanes per
  * line, kU nonzeros in flight per lane; kLPR = 0 is the slab form (the
  * gathered block staged through shared memory a slab at a time, kw/4 lanes
- * per line); kLPR = -1 the units form (blocks of 4 or 8: the block's rows
- * staged per slab in shared memory, the matrix in the FP32 unit layout with
- * 16-bit slab-local indices, a lane per line).  Returns PLSQR_ERR_ARG past
- * the last. */
+ * per line); kLPR = -1 the units form (passes of 4 or 8 columns: the
+ * block's rows staged per slab in shared memory, the matrix in the FP32 unit
+ * layout with 16-bit slab-local indices, a lane per line).  Returns
+ * PLSQR_ERR_ARG past the last. */
 int plsqr_batch_variant(int32_t index, int32_t *vw, int32_t *lanes_per_line,
                         int32_t *unroll);
 

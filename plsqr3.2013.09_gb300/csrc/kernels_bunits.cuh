@@ -31,7 +31,7 @@ template <int KW>
 __global__ void __launch_bounds__(kBUnitThreads, 1)
     k_bunits(UnitsArgs<float> A, int *__restrict__ next, const float *__restrict__ xf, int kp,
              int col0, double *__restrict__ partial) {
-  static_assert(KW == 4 || KW == 8, "blocks of 4 or 8 right-hand sides");
+  static_assert(KW == 4 || KW == 8, "passes of 4 or 8 columns");
   constexpr int V4 = KW / 4;  // float4 pieces of a row
   constexpr int P = UnitPieces<float>::P;
   extern __shared__ __align__(16) float4 xs4[];

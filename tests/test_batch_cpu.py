@@ -64,4 +64,4 @@ def test_variant_table(pkg):
     assert len(seen) == 14 and len(set(seen)) == 14
     assert all(vw in (2, 4) and lpr in (8, 16, 32) and u in (2, 4) for vw, lpr, u in seen[:12])
     assert seen[12] == (4, 0, 0)  # the slab form
-    assert seen[13] == (4, -1, 0)  # the units form (blocks of 4 or 8)
+    assert seen[13] == (4, -1, 0)  # the units form (passes of 4 or 8 columns)
