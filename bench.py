@@ -361,11 +361,15 @@ def main() -> int:
     bytes_dom = info[f"hbm_bytes_aprod{dom_mode}"]
     peak, peak_kind = measured_peaks()
     achieved = bytes_dom / (ms_dom * 1e-3) / 1e9
-    kname = "k_aprod2" if dom_mode == 2 else "k_aprod1"
+    # the products as launched: the unit kernel over the slabs of the kernel
+    # rows (mode 1) or columns (mode 2) and the kernel that adds the slab
+    # partials with the damping part and the LSQR scaling
+    kernels = {1: "aprod mode 1 (A x): k_slab_units<double> over K rows + k_combine_rows",
+               2: "aprod mode 2 (A^T y): k_slab_units<double> over K columns + k_combine_cols"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": ncu_traffic(kname),
-                "kernel": kname, "peak_kind": peak_kind,
-                "ms_per_launch": {"k_aprod1": ms1, "k_aprod2": ms2, "iteration": ms_it},
+                "frac": achieved / peak, "traffic": ncu_traffic(f"aprod_mode{dom_mode}"),
+                "kernel": kernels[dom_mode], "peak_kind": peak_kind,
+                "ms_per_launch": {"aprod_mode1": ms1, "aprod_mode2": ms2, "iteration": ms_it},
                 "bytes_per_launch": bytes_dom}
 
     extra = {}
